@@ -1,0 +1,95 @@
+// Kernel argument block shared by the host runtime (g++/nvcc) and the
+// NVRTC-compiled ensemble kernels.  Passed by value to every kernel, so the
+// solver and observer parameters sit in the constant bank rather than in
+// global memory.  No includes: NVRTC compiles it without system headers.
+//
+// SolverParams / ObserverParams keep the field order and meaning of
+// clode/cpp/clODE_struct_defs.cl:11-20 and clode/cpp/observers.cl:25-46.
+#pragma once
+
+namespace clode {
+
+template <typename R>
+struct SolverParamsT {
+    R dt;
+    R dtmax;
+    R abstol;
+    R reltol;
+    unsigned int max_steps;
+    unsigned int max_store;
+    unsigned int nout;
+};
+
+template <typename R>
+struct ObserverParamsT {
+    unsigned int eVarIx;
+    unsigned int fVarIx;
+    unsigned int maxEventCount;
+    unsigned int maxEventTimestamps;
+    R minXamp;
+    R minIMI;
+    R nHoodRadius;
+    R xUpThresh;
+    R xDownThresh;
+    R dxUpThresh;
+    R dxDownThresh;
+    R eps_dx;
+};
+
+// Per-member status bits (written to ArgsT::status when it is non-null)
+enum StatusBits {
+    STATUS_HMIN_FAIL = 1,       // an adaptive step hit hmin with error above tolerance
+    STATUS_NONFINITE = 2,       // the final state holds a NaN or Inf
+    STATUS_MAX_STEPS = 4,       // the loop stopped on max_steps before reaching t1
+    STATUS_TERMINAL_EVENT = 8,  // the observer's event limit ended the run
+    STATUS_TIME_BUDGET = 16,    // the persistent launch ran out of its time budget
+};
+
+// Launch-wide counters (ArgsT::stats, 64-bit, accumulated with atomics)
+enum StatsSlots {
+    STAT_STEPS = 0,        // accepted steps
+    STAT_REJECTED = 1,     // rejected adaptive attempts
+    STAT_RHS_EVALS = 2,    // right-hand-side evaluations, all passes
+    STAT_EVENTS = 3,       // observer events
+    STAT_MEMBERS = 4,      // members finished
+    STAT_COUNT = 8
+};
+
+template <typename R>
+struct ArgsT {
+    // ensemble geometry: SoA stride and the member range this launch covers
+    int nPts;
+    int i_begin;
+    int i_end;
+    int fused_init;            // features: run the observer initialisation in the same launch
+    // time span: global [t0, t1] or, when tspan_pm != 0, per member [2*i], [2*i+1]
+    R t0;
+    R t1;
+    const R *tspan_pm;
+    // problem data, SoA [j * nPts + i]
+    const R *x0;
+    const R *pars;
+    R *xf;
+    unsigned long long *rng;   // [2 * nPts]
+    R *dt;                     // [nPts], read at start, written at end
+    R *tf;                     // [nPts]
+    // observer state, SoA in 32-bit words [w * nPts + i], and features [k * nPts + i]
+    unsigned int *odata;
+    R *F;
+    // trajectory output, [row * nPts * n + j * nPts + i]
+    R *t_out;
+    R *x_out;
+    R *dx_out;
+    R *aux_out;
+    int *n_stored;
+    // optional diagnostics (may be null)
+    int *status;
+    unsigned long long *stats;
+    // persistent scheduling: next member to hand out, and a %globaltimer budget in ns (0 = none)
+    unsigned int *work_next;
+    unsigned long long time_budget_ns;
+    SolverParamsT<R> sp;
+    ObserverParamsT<R> op;
+};
+
+}  // namespace clode

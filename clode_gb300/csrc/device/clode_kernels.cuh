@@ -1,0 +1,317 @@
+// Ensemble kernels: transient, trajectory, observer initialisation and
+// features, one ensemble member per thread with all of its state in
+// registers.  Entry points come in two schedules:
+//
+//  * grid:       one thread per member of [i_begin, i_end), blocks of
+//                blockDim.x threads.  The direct counterpart of the
+//                reference's NDRange(nPts) launch (clode/cpp/CLODE.cpp:484).
+//  * persistent: a fixed grid (a multiple of the SM count) whose lanes pull
+//                members from a global counter one at a time.  A lane whose
+//                member finishes early refills itself immediately, so
+//                members of very different lengths (adaptive steps,
+//                per-member time spans, terminal events, two-pass observers)
+//                keep every lane busy.  Both passes of a two-pass observer
+//                run through the same stepper call, so lanes in different
+//                passes stay converged on the expensive part of the loop.
+//
+// Per member, both schedules execute the same arithmetic in the same order,
+// so their results are identical.  Member semantics follow
+// clode/cpp/transient.cl:9-77, initializeObserver.cl:9-84, features.cl:10-106
+// and trajectory.cl:14-112.
+#pragma once
+
+namespace clode {
+
+typedef ArgsT<realtype> Args;
+
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ realtype member_t0(const Args &a, int i)
+{
+    return a.tspan_pm ? a.tspan_pm[2ull * i] : a.t0;
+}
+
+__device__ __forceinline__ realtype member_t1(const Args &a, int i)
+{
+    return a.tspan_pm ? a.tspan_pm[2ull * i + 1] : a.t1;
+}
+
+__device__ __forceinline__ void load_x0(realtype (&x)[N_VAR], const Args &a, int i)
+{
+    const unsigned long long n = (unsigned long long)a.nPts;
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j)
+        x[j] = a.x0[j * n + i];
+}
+
+// private copies and the slope at the initial point (transient.cl:20-51)
+__device__ __forceinline__ void member_load(Member &m, const Args &a, int i, Counters &c)
+{
+    const unsigned long long n = (unsigned long long)a.nPts;
+    m.t = member_t0(a, i);
+    m.dt = a.dt[i];
+#pragma unroll
+    for (int j = 0; j < N_PAR; ++j)
+        m.p[j] = a.pars[j * n + i];
+    load_x0(m.x, a, i);
+#pragma unroll
+    for (int j = 0; j < NW1; ++j)
+        m.w[j] = ZERO;
+#pragma unroll
+    for (int j = 0; j < NA1; ++j)
+        m.aux[j] = ZERO;
+#if CLODE_STOCHASTIC
+    m.r.s0 = a.rng[i];
+    m.r.s1 = a.rng[n + i];
+    m.r.have_spare = false;
+    m.r.spare = ZERO;
+#pragma unroll
+    for (int j = 0; j < N_WIENER; ++j)
+        m.w[j] = rng_normal(m.r) / sqrt(m.dt);
+#endif
+    getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
+    c.rhs += 1;
+}
+
+// final state, RNG state, step size and time (transient.cl:64-76).  Only
+// the stochastic stepper draws numbers, so the stored RNG state of the other
+// steppers is the loaded one and is left untouched in global memory.
+__device__ __forceinline__ void member_store(const Member &m, const Args &a, int i)
+{
+    const unsigned long long n = (unsigned long long)a.nPts;
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j)
+        a.xf[j * n + i] = m.x[j];
+#if CLODE_STOCHASTIC
+    a.rng[i] = m.r.s0;
+    a.rng[n + i] = m.r.s1;
+#endif
+    a.dt[i] = m.dt;
+    a.tf[i] = m.t;
+}
+
+__device__ __forceinline__ int member_status_bits(const Member &m, unsigned int step, const Args &a,
+                                                  realtype t1, bool hmin_fail, bool terminal)
+{
+    int s = 0;
+    if (hmin_fail) s |= STATUS_HMIN_FAIL;
+    if (terminal) s |= STATUS_TERMINAL_EVENT;
+    bool finite = isfinite(m.t);
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j)
+        finite = finite && isfinite(m.x[j]);
+    if (!finite) s |= STATUS_NONFINITE;
+    if (!terminal && step >= a.sp.max_steps && m.t <= t1) s |= STATUS_MAX_STEPS;
+    return s;
+}
+
+// Sum per-thread counters over the warp and add them to the launch totals.
+// Must be reached by every lane of the warp.
+__device__ __forceinline__ void flush_counters(const Args &a, const Counters &c)
+{
+    if (!a.stats)
+        return;
+    unsigned long long v[4] = {c.steps, c.rejected, c.rhs, c.events};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+            v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&a.stats[STAT_STEPS], v[0]);
+        atomicAdd(&a.stats[STAT_REJECTED], v[1]);
+        atomicAdd(&a.stats[STAT_RHS_EVALS], v[2]);
+        atomicAdd(&a.stats[STAT_EVENTS], v[3]);
+    }
+}
+
+// ------------------------------------------------------------- transient --
+__device__ __forceinline__ void run_transient(const Args &a, int i, Counters &c)
+{
+    Member m;
+    member_load(m, a, i, c);
+    const realtype t1 = member_t1(a, i);
+    unsigned int step = 0;
+    bool hmin_fail = false;
+    while (m.t <= t1 && step < a.sp.max_steps) {
+        ++step;
+        hmin_fail |= step_member(m, a.sp, t1, c) != 0;
+    }
+    member_store(m, a, i);
+    if (a.status)
+        a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, false);
+}
+
+extern "C" __global__ void clode_transient(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.i_end)
+        run_transient(a, i, c);
+    flush_counters(a, c);
+}
+
+// ------------------------------------------------------------ trajectory --
+__device__ __forceinline__ void store_row(const Args &a, const Member &m, int i, unsigned long long row)
+{
+    const unsigned long long n = (unsigned long long)a.nPts;
+    a.t_out[row * n + i] = m.t;
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j)
+        a.x_out[row * n * N_VAR + j * n + i] = m.x[j];
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j)
+        a.dx_out[row * n * N_VAR + j * n + i] = m.dx[j];
+#pragma unroll
+    for (int j = 0; j < N_AUX; ++j)
+        a.aux_out[row * n * N_AUX + j * n + i] = m.aux[j];
+}
+
+__device__ __forceinline__ void run_trajectory(const Args &a, int i, Counters &c)
+{
+    Member m;
+    member_load(m, a, i, c);
+    const realtype t1 = member_t1(a, i);
+    unsigned long long row = 0;
+    store_row(a, m, i, row);
+    unsigned int step = 0;
+    bool hmin_fail = false;
+    while (m.t <= t1 && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store) {
+        ++step;
+        hmin_fail |= step_member(m, a.sp, t1, c) != 0;
+        if (step % a.sp.nout == 0) {
+            ++row;
+            store_row(a, m, i, row);
+        }
+    }
+    a.n_stored[i] = (int)row;
+    member_store(m, a, i);
+    if (a.status)
+        a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, false);
+}
+
+extern "C" __global__ void clode_trajectory(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.i_end)
+        run_trajectory(a, i, c);
+    flush_counters(a, c);
+}
+
+#if CLODE_HAVE_OBSERVER
+// --------------------------------------------------- parked observer state --
+static_assert(sizeof(Observer) % 4 == 0, "observer state must be a whole number of 32-bit words");
+#define CLODE_OBS_WORDS ((int)(sizeof(Observer) / 4))
+
+// read by the host to size the parked-state buffer
+extern "C" __device__ const unsigned int clode_observer_words = CLODE_OBS_WORDS;
+
+__device__ __forceinline__ void park_load(Observer &o, const Args &a, int i)
+{
+    const unsigned long long n = (unsigned long long)a.nPts;
+    unsigned int w[CLODE_OBS_WORDS];
+#pragma unroll
+    for (int k = 0; k < CLODE_OBS_WORDS; ++k)
+        w[k] = a.odata[k * n + i];
+    memcpy(&o, w, sizeof(Observer));
+}
+
+__device__ __forceinline__ void park_store(const Observer &o, const Args &a, int i)
+{
+    const unsigned long long n = (unsigned long long)a.nPts;
+    unsigned int w[CLODE_OBS_WORDS];
+    memcpy(w, &o, sizeof(Observer));
+#pragma unroll
+    for (int k = 0; k < CLODE_OBS_WORDS; ++k)
+        a.odata[k * n + i] = w[k];
+}
+
+// Observer initialisation for one member (initializeObserver.cl:9-84).
+// The member's RNG state and dt are not written back.
+__device__ __forceinline__ void init_observer_member(Observer &o, const Args &a, int i, Counters &c)
+{
+    Member m;
+    member_load(m, a, i, c);
+    o.init(m.t, m.x, m.dx, m.aux, a.op);
+    if (Observer::two_pass) {
+        const realtype t1 = member_t1(a, i);
+        unsigned int step = 0;
+        while (m.t < t1 && step < a.sp.max_steps) {
+            ++step;
+            step_member(m, a.sp, t1, c);
+            o.warmup(m.t, m.x, m.dx, m.aux, a.op);
+        }
+        // rewind to the initial state (the last noise sample is kept)
+        m.t = member_t0(a, i);
+        load_x0(m.x, a, i);
+        getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
+        c.rhs += 1;
+    }
+    o.arm(m.t, m.x, m.dx, m.aux, a.op);
+}
+
+extern "C" __global__ void clode_init_observer(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.i_end) {
+        Observer o;
+        init_observer_member(o, a, i, c);
+        park_store(o, a, i);
+    }
+    flush_counters(a, c);
+}
+
+// Feature pass for one member (features.cl:10-106)
+__device__ __forceinline__ void features_member(Observer &o, const Args &a, int i, Counters &c)
+{
+    Member m;
+    member_load(m, a, i, c);
+    const realtype t0 = m.t;
+    const realtype t1 = member_t1(a, i);
+    unsigned int step = 0;
+    bool hmin_fail = false, terminal = false;
+    while (m.t <= t1 && step < a.sp.max_steps) {
+        ++step;
+        hmin_fail |= step_member(m, a.sp, t1, c) != 0;
+        o.update(m.t, m.x, m.dx, m.aux, a.op);
+        if (o.event(m.t, m.x, m.dx, m.aux, a.op)) {
+            c.events++;
+            if (o.on_event(m.t, m.x, m.dx, m.aux, a.op)) {
+                terminal = true;
+                break;
+            }
+        }
+    }
+    FOut out = {a.F, (unsigned long long)a.nPts, i, 0};
+    o.write(out);
+    o.rebase(m.t - t0);
+    member_store(m, a, i);
+    if (a.status)
+        a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, terminal);
+}
+
+extern "C" __global__ void clode_features(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.i_end) {
+        Observer o;
+        if (a.fused_init)
+            init_observer_member(o, a, i, c);
+        else
+            park_load(o, a, i);
+        features_member(o, a, i, c);
+        park_store(o, a, i);
+    }
+    flush_counters(a, c);
+}
+#endif  // CLODE_HAVE_OBSERVER
+
+}  // namespace clode

@@ -1,0 +1,747 @@
+// On-the-fly feature observers.  One observer is compiled in per program
+// (USE_OBSERVER_*).  Its state is a plain struct held in registers for the
+// whole time loop; between launches it is parked in global memory as 32-bit
+// words in SoA order ([word * nPts + member]) so that loads and stores
+// coalesce across a warp.  That layout is private to this engine; only the
+// feature vector F has a public layout (F[k * nPts + i], k in the order of
+// the reference's feature-name lists).
+//
+// Hook semantics and arithmetic follow the reference observers:
+//   basic     clode/cpp/observers/observer_basic.clh:21-90
+//   basicall  clode/cpp/observers/observer_basic_allVar.clh:35-130
+//   localmax  clode/cpp/observers/observer_local_maximum.clh:54-328
+//   nhood1    clode/cpp/observers/observer_neighborhood_1.clh:44-364
+//   nhood2    clode/cpp/observers/observer_neighborhood_2.clh:50-313
+//   thresh2   clode/cpp/observers/observer_threshold_2.clh:63-470
+// The reference keeps a 3-step solution buffer as [var * 3 + slot]; here it is
+// one array per slot (b0 oldest, b2 newest), which holds the same values.
+// The event and feature variables (eVarIx, fVarIx) are runtime values, so
+// the buffers are read through unrolled selects that keep them in registers.
+#pragma once
+
+namespace clode {
+
+typedef ObserverParamsT<realtype> ObserverParams;
+
+#define NSE1 (N_STORE_EVENTS > 0 ? N_STORE_EVENTS : 1)
+
+template <int N>
+__device__ __forceinline__ realtype sel(const realtype (&a)[N], unsigned int ix)
+{
+    realtype v = a[0];
+#pragma unroll
+    for (int k = 1; k < N; ++k)
+        if (ix == (unsigned int)k)
+            v = a[k];
+    return v;
+}
+
+template <int N>
+__device__ __forceinline__ void put(realtype (&a)[N], unsigned int ix, realtype v)
+{
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        if (ix == (unsigned int)k)
+            a[k] = v;
+}
+
+// running means, clode/cpp/clODE_utilities.cl:167-177
+__device__ __forceinline__ realtype mean_time(realtype mean, realtype v, realtype dt, realtype elapsed)
+{
+    return mean + (v - mean) * dt / elapsed;
+}
+
+__device__ __forceinline__ void mean_count(realtype &mean, realtype v, unsigned int n)
+{
+    if (n == 1)
+        mean = v;
+    else if (n > 1)
+        mean += (v - mean) / (realtype)n;
+}
+
+// first-occurrence arg-extremum of three values, clODE_utilities.cl:49-127
+__device__ __forceinline__ int argmax3(realtype a, realtype b, realtype c)
+{
+    realtype best = -BIG_REAL;
+    int ix = 0;
+    if (a > best) { best = a; ix = 0; }
+    if (b > best) { best = b; ix = 1; }
+    if (c > best) { best = c; ix = 2; }
+    return ix;
+}
+
+__device__ __forceinline__ int argmin3(realtype a, realtype b, realtype c)
+{
+    realtype best = BIG_REAL;
+    int ix = 0;
+    if (a < best) { best = a; ix = 0; }
+    if (b < best) { best = b; ix = 1; }
+    if (c < best) { best = c; ix = 2; }
+    return ix;
+}
+
+__device__ __forceinline__ realtype pick3(int ix, realtype a, realtype b, realtype c)
+{
+    return ix == 0 ? a : (ix == 1 ? b : c);
+}
+
+// max / min / mean triple over events or periods
+struct Stat3 {
+    realtype hi, lo, mean;
+    __device__ __forceinline__ void reset() { hi = -BIG_REAL; lo = BIG_REAL; mean = ZERO; }
+    __device__ __forceinline__ void push(realtype v, unsigned int n)
+    {
+        hi = fmax(v, hi);
+        lo = fmin(v, lo);
+        mean_count(mean, v, n);
+    }
+};
+
+// 3-step solution buffer
+struct SolBuf {
+    realtype t0, t1, t2;
+    realtype x0[N_VAR], x1[N_VAR], x2[N_VAR];
+    realtype d0[N_VAR], d1[N_VAR], d2[N_VAR];
+    __device__ __forceinline__ void seed(realtype t, const realtype (&x)[N_VAR], const realtype (&dx)[N_VAR])
+    {
+        t2 = t;
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            x2[j] = x[j];
+            d2[j] = dx[j];
+        }
+    }
+    __device__ __forceinline__ void shift(realtype t, const realtype (&x)[N_VAR], const realtype (&dx)[N_VAR])
+    {
+        t0 = t1; t1 = t2; t2 = t;
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            x0[j] = x1[j]; x1[j] = x2[j]; x2[j] = x[j];
+            d0[j] = d1[j]; d1[j] = d2[j]; d2[j] = dx[j];
+        }
+    }
+    __device__ __forceinline__ void rebase(realtype T) { t0 -= T; t1 -= T; t2 -= T; }
+};
+
+// whole-trajectory extent of every state variable, its slope and every aux
+struct Extent {
+    realtype xmax[N_VAR], xmin[N_VAR], xmean[N_VAR], dxmax[N_VAR], dxmin[N_VAR];
+    realtype amax[NA1], amin[NA1], amean[NA1];
+    __device__ __forceinline__ void reset()
+    {
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            xmax[j] = -BIG_REAL; xmin[j] = BIG_REAL; xmean[j] = ZERO;
+            dxmax[j] = -BIG_REAL; dxmin[j] = BIG_REAL;
+        }
+#pragma unroll
+        for (int j = 0; j < N_AUX; ++j) {
+            amax[j] = -BIG_REAL; amin[j] = BIG_REAL; amean[j] = ZERO;
+        }
+    }
+    __device__ __forceinline__ void update(const realtype (&x)[N_VAR], const realtype (&dx)[N_VAR],
+                                           const realtype (&aux)[NA1], realtype dt, realtype elapsed)
+    {
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            xmax[j] = fmax(x[j], xmax[j]);
+            xmin[j] = fmin(x[j], xmin[j]);
+            xmean[j] = mean_time(xmean[j], x[j], dt, elapsed);
+            dxmax[j] = fmax(dx[j], dxmax[j]);
+            dxmin[j] = fmin(dx[j], dxmin[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_AUX; ++j) {
+            amax[j] = fmax(aux[j], amax[j]);
+            amin[j] = fmin(aux[j], amin[j]);
+            amean[j] = mean_time(amean[j], aux[j], dt, elapsed);
+        }
+    }
+};
+
+// feature writer: F[k * nPts + i]
+struct FOut {
+    realtype *F;
+    unsigned long long stride;
+    int i;
+    int k;
+    __device__ __forceinline__ void operator()(realtype v)
+    {
+        F[(unsigned long long)k * stride + i] = v;
+        ++k;
+    }
+};
+
+#define CLODE_HOOK_ARGS realtype t, const realtype (&x)[N_VAR], const realtype (&dx)[N_VAR], \
+                        const realtype (&aux)[NA1], const ObserverParams &op
+
+#if defined(USE_OBSERVER_BASIC)
+#define CLODE_HAVE_OBSERVER 1
+struct Observer {
+    static constexpr bool two_pass = false;
+    realtype xmax, xmin, xmean, dxmax, dxmin, t_last, t_start;
+    unsigned int steps;
+
+    __device__ __forceinline__ void init(CLODE_HOOK_ARGS)
+    {
+        xmax = -BIG_REAL; xmin = BIG_REAL; xmean = ZERO; dxmax = -BIG_REAL; dxmin = BIG_REAL;
+        t_last = t; t_start = t; steps = 0;
+    }
+    __device__ __forceinline__ void warmup(CLODE_HOOK_ARGS) {}
+    __device__ __forceinline__ void arm(CLODE_HOOK_ARGS) {}
+    __device__ __forceinline__ void update(CLODE_HOOK_ARGS)
+    {
+        ++steps;
+        realtype h = t - t_last;
+        t_last = t;
+        realtype elapsed = t - t_start;
+        realtype xf = sel(x, op.fVarIx), df = sel(dx, op.fVarIx);
+        xmax = fmax(xf, xmax);
+        xmin = fmin(xf, xmin);
+        xmean = mean_time(xmean, xf, h, elapsed);
+        dxmax = fmax(df, dxmax);
+        dxmin = fmin(df, dxmin);
+    }
+    __device__ __forceinline__ bool event(CLODE_HOOK_ARGS) { return false; }
+    __device__ __forceinline__ bool on_event(CLODE_HOOK_ARGS) { return false; }
+    __device__ __forceinline__ void write(FOut &o) const
+    {
+        o(xmax); o(xmin); o(xmean); o(dxmax); o(dxmin); o((realtype)steps);
+    }
+    __device__ __forceinline__ void rebase(realtype T) { t_start -= T; }
+};
+
+#elif defined(USE_OBSERVER_BASIC_ALLVAR)
+#define CLODE_HAVE_OBSERVER 1
+struct Observer {
+    static constexpr bool two_pass = false;
+    Extent ext;
+    realtype t_last, t_start;
+    unsigned int steps;
+
+    __device__ __forceinline__ void init(CLODE_HOOK_ARGS)
+    {
+        ext.reset();
+        t_last = t; t_start = t; steps = 0;
+    }
+    __device__ __forceinline__ void warmup(CLODE_HOOK_ARGS) {}
+    __device__ __forceinline__ void arm(CLODE_HOOK_ARGS) {}
+    __device__ __forceinline__ void update(CLODE_HOOK_ARGS)
+    {
+        ++steps;
+        realtype h = t - t_last;
+        t_last = t;
+        ext.update(x, dx, aux, h, t - t_start);
+    }
+    __device__ __forceinline__ bool event(CLODE_HOOK_ARGS) { return false; }
+    __device__ __forceinline__ bool on_event(CLODE_HOOK_ARGS) { return false; }
+    __device__ __forceinline__ void write(FOut &o) const
+    {
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xmean[j]); o(ext.dxmax[j]); o(ext.dxmin[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_AUX; ++j) {
+            o(ext.amax[j]); o(ext.amin[j]); o(ext.amean[j]);
+        }
+        o((realtype)steps);
+    }
+    __device__ __forceinline__ void rebase(realtype T) { t_start -= T; }
+};
+
+#elif defined(USE_OBSERVER_LOCAL_MAX)
+#define CLODE_HAVE_OBSERVER 1
+struct Observer {
+    static constexpr bool two_pass = false;
+    SolBuf b;
+    Extent ext;
+    realtype tmax_list[NSE1], xmax_list[NSE1], tmin_list[NSE1], xmin_list[NSE1];
+    Stat3 imi, amp;
+    realtype t_start, t_last_max, t_last_min, x_last_min;
+    unsigned int events, steps;
+
+    __device__ __forceinline__ void init(CLODE_HOOK_ARGS)
+    {
+        b.seed(t, x, dx);
+        ext.reset();
+#pragma unroll
+        for (int j = 0; j < NSE1; ++j)
+            tmax_list[j] = xmax_list[j] = tmin_list[j] = xmin_list[j] = ZERO;
+        imi.reset();
+        amp.reset();
+        t_start = t; t_last_max = ZERO; t_last_min = ZERO; x_last_min = BIG_REAL;
+        events = 0; steps = 0;
+    }
+    __device__ __forceinline__ void warmup(CLODE_HOOK_ARGS) {}
+    __device__ __forceinline__ void arm(CLODE_HOOK_ARGS) {}
+    __device__ __forceinline__ void update(CLODE_HOOK_ARGS)
+    {
+        ++steps;
+        b.shift(t, x, dx);
+        realtype h = b.t2 - b.t1;
+        ext.update(x, dx, aux, h, t - t_start);
+        if (steps < 2)
+            return;
+        const unsigned int f = op.fVarIx;
+        if (sel(b.d1, f) < ZERO && sel(b.d2, f) > ZERO) {
+            realtype a0 = sel(b.x0, f), a1 = sel(b.x1, f), a2 = sel(b.x2, f);
+            int ix = argmin3(a0, a1, a2);
+            t_last_min = pick3(ix, b.t0, b.t1, b.t2);
+            x_last_min = pick3(ix, a0, a1, a2);
+            // A minimum before the first maximum (events == 0) is not stored:
+            // the reference's unsigned index events-1 points outside the list.
+            if (events > 0 && events <= N_STORE_EVENTS) {
+                put(tmin_list, events - 1, t_last_min);
+                put(xmin_list, events - 1, x_last_min);
+            }
+        }
+    }
+    __device__ __forceinline__ bool event(CLODE_HOOK_ARGS)
+    {
+        if (steps < 2)
+            return false;
+        return sel(b.d1, op.fVarIx) > ZERO && sel(b.d2, op.fVarIx) < ZERO;
+    }
+    __device__ __forceinline__ bool on_event(CLODE_HOOK_ARGS)
+    {
+        const unsigned int f = op.fVarIx;
+        realtype a0 = sel(b.x0, f), a1 = sel(b.x1, f), a2 = sel(b.x2, f);
+        int ix = argmax3(a0, a1, a2);
+        realtype tpk = pick3(ix, b.t0, b.t1, b.t2), xpk = pick3(ix, a0, a1, a2);
+        ++events;
+        if (events > 1) {
+            imi.push(tpk - t_last_max, events - 1);
+            amp.push(xpk - x_last_min, events - 1);
+        }
+        t_last_max = tpk;
+        if (events <= N_STORE_EVENTS) {
+            put(tmax_list, events - 1, tpk);
+            put(xmax_list, events - 1, xpk);
+        }
+        return events == op.maxEventCount;
+    }
+    __device__ __forceinline__ void write(FOut &o) const
+    {
+        bool two = events > 1;
+        o(two ? imi.hi : ZERO); o(two ? imi.lo : ZERO); o(two ? imi.mean : ZERO);
+        o(two ? amp.hi : ZERO); o(two ? amp.lo : ZERO); o(two ? amp.mean : ZERO);
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xmean[j]); o(ext.dxmax[j]); o(ext.dxmin[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_AUX; ++j) {
+            o(ext.amax[j]); o(ext.amin[j]); o(ext.amean[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_STORE_EVENTS; ++j) {
+            o(tmax_list[j]); o(xmax_list[j]); o(tmin_list[j]); o(xmin_list[j]);
+        }
+        o((realtype)events);
+        o((realtype)steps);
+    }
+    __device__ __forceinline__ void rebase(realtype T)
+    {
+        t_start -= T;
+        t_last_max = t_last_max - T;
+        t_last_min = t_last_min - T;
+        b.rebase(T);
+    }
+};
+
+#elif defined(USE_OBSERVER_NEIGHBORHOOD_1)
+#define CLODE_HAVE_OBSERVER 1
+struct Observer {
+    static constexpr bool two_pass = false;
+    SolBuf b;
+    realtype c[N_VAR];  // neighbourhood centre
+    Extent ext;
+    Stat3 npk, period, hstat;
+    realtype t_start, t_last_event, norm_now, norm_prev;
+    unsigned int peaks_now, events, steps, have_c, inside;
+
+    __device__ __forceinline__ void init(CLODE_HOOK_ARGS)
+    {
+        b.seed(t, x, dx);
+        ext.reset();
+        npk.reset(); period.reset(); hstat.reset();
+        // never read before being set; cleared so the parked state is defined
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            c[j] = ZERO;
+        t_start = t; t_last_event = ZERO; norm_now = ZERO; norm_prev = ZERO;
+        peaks_now = 0; events = 0; steps = 0; have_c = 0; inside = 0;
+    }
+    __device__ __forceinline__ void warmup(CLODE_HOOK_ARGS) {}
+    __device__ __forceinline__ void arm(CLODE_HOOK_ARGS) {}
+    __device__ __forceinline__ void update(CLODE_HOOK_ARGS)
+    {
+        ++steps;
+        b.shift(t, x, dx);
+        realtype h = b.t2 - b.t1;
+        hstat.push(h, steps);
+        // per-step (not time-weighted) means in this observer
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            ext.xmax[j] = fmax(x[j], ext.xmax[j]);
+            ext.xmin[j] = fmin(x[j], ext.xmin[j]);
+            mean_count(ext.xmean[j], x[j], steps);
+            ext.dxmax[j] = fmax(dx[j], ext.dxmax[j]);
+            ext.dxmin[j] = fmin(dx[j], ext.dxmin[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_AUX; ++j) {
+            ext.amax[j] = fmax(aux[j], ext.amax[j]);
+            ext.amin[j] = fmin(aux[j], ext.amin[j]);
+            mean_count(ext.amean[j], aux[j], steps);
+        }
+        if (steps > 1) {
+            const unsigned int e = op.eVarIx, f = op.fVarIx;
+            if (!have_c) {
+                if (sel(b.d1, e) <= ZERO && sel(b.d2, e) > ZERO) {
+                    int ix = argmin3(sel(b.x0, e), sel(b.x1, e), sel(b.x2, e));
+                    t_last_event = pick3(ix, b.t0, b.t1, b.t2);
+                    have_c = 1;
+#pragma unroll
+                    for (int j = 0; j < N_VAR; ++j)
+                        c[j] = pick3(ix, b.x0[j], b.x1[j], b.x2[j]);
+                }
+            } else if (sel(b.d1, f) >= ZERO && sel(b.d2, f) < ZERO) {
+                peaks_now++;
+            }
+        }
+    }
+    __device__ __forceinline__ bool event(CLODE_HOOK_ARGS)
+    {
+        if (steps < 2 || !have_c)
+            return false;
+        const unsigned int f = op.fVarIx;
+        if (sel(ext.xmax, f) - sel(ext.xmin, f) < op.minXamp)
+            return false;
+        unsigned int was_inside = inside;
+        norm_prev = norm_now;
+        realtype acc = ZERO;
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            realtype d = fabs(x[j] - c[j]) / (ext.xmax[j] - ext.xmin[j]);
+            acc += d * d;
+        }
+        norm_now = sqrt(acc);
+        inside = norm_now <= op.nHoodRadius;
+        return inside && !was_inside;
+    }
+    __device__ __forceinline__ bool on_event(CLODE_HOOK_ARGS)
+    {
+        ++events;
+        if (events > 1) {
+            npk.push((realtype)peaks_now, events - 1);
+            period.push(t - t_last_event, events - 1);
+        }
+        t_last_event = t;
+        peaks_now = 0;
+        return events >= op.maxEventCount;
+    }
+    __device__ __forceinline__ void write(FOut &o) const
+    {
+        bool two = events > 1;
+        o(two ? period.hi : ZERO); o(two ? period.lo : ZERO); o(two ? period.mean : ZERO);
+        o(two ? npk.hi : ZERO); o(two ? npk.lo : ZERO); o(two ? npk.mean : ZERO);
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xmean[j]); o(ext.dxmax[j]); o(ext.dxmin[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_AUX; ++j) {
+            o(ext.amax[j]); o(ext.amin[j]); o(ext.amean[j]);
+        }
+        o((realtype)(events - 1u));  // "period count", unsigned as in the reference
+        o((realtype)steps);
+        o(hstat.hi); o(hstat.lo); o(hstat.mean);
+    }
+    __device__ __forceinline__ void rebase(realtype T)
+    {
+        t_start -= T;
+        t_last_event -= T;
+        b.rebase(T);
+    }
+};
+
+#elif defined(USE_OBSERVER_NEIGHBORHOOD_2)
+#define CLODE_HAVE_OBSERVER 1
+struct Observer {
+    static constexpr bool two_pass = true;
+    SolBuf b;
+    realtype c[N_VAR];  // neighbourhood centre
+    Extent ext;
+    realtype xrange[N_VAR];
+    realtype tex_list[NSE1];
+    Stat3 npk, period, hstat;
+    realtype t_start, t_last_event, x_thresh;
+    unsigned int peaks_now, have_c, inside, events, steps;
+
+    __device__ __forceinline__ void init(CLODE_HOOK_ARGS)
+    {
+        b.seed(t, x, dx);
+        ext.reset();
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            c[j] = x[j];
+            xrange[j] = ZERO;
+        }
+#pragma unroll
+        for (int j = 0; j < NSE1; ++j)
+            tex_list[j] = ZERO;
+        npk.reset(); period.reset(); hstat.reset();
+        t_start = t; t_last_event = ZERO; x_thresh = ZERO;
+        peaks_now = 0; have_c = 0; inside = 0; events = 0; steps = 0;
+    }
+    // first pass: extent of every state variable
+    __device__ __forceinline__ void warmup(CLODE_HOOK_ARGS)
+    {
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            ext.xmax[j] = fmax(x[j], ext.xmax[j]);
+            ext.xmin[j] = fmin(x[j], ext.xmin[j]);
+        }
+    }
+    __device__ __forceinline__ void arm(CLODE_HOOK_ARGS)
+    {
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            xrange[j] = ext.xmax[j] - ext.xmin[j];
+        x_thresh = sel(ext.xmin, op.eVarIx) + op.xDownThresh * sel(xrange, op.eVarIx);
+    }
+    __device__ __forceinline__ void update(CLODE_HOOK_ARGS)
+    {
+        ++steps;
+        b.shift(t, x, dx);
+        realtype h = b.t2 - b.t1;
+        hstat.push(h, steps);
+        ext.update(x, dx, aux, h, t - t_start);
+        if (steps < 2)
+            return;
+        if (have_c) {
+            if (sel(b.d1, op.fVarIx) >= ZERO && sel(b.d2, op.fVarIx) < ZERO)
+                peaks_now++;
+            return;
+        }
+        // centre: first downward crossing of the event variable's threshold
+        if (sel(b.x1, op.eVarIx) > x_thresh && sel(b.x2, op.eVarIx) < x_thresh) {
+            have_c = 1;
+            inside = 1;
+#pragma unroll
+            for (int j = 0; j < N_VAR; ++j)
+                c[j] = x[j];
+        }
+    }
+    // event: exit from the L2 ball around c in range-normalised coordinates
+    __device__ __forceinline__ bool event(CLODE_HOOK_ARGS)
+    {
+        if (steps < 2 || !have_c)
+            return false;
+        realtype acc = ZERO;
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            realtype d = (x[j] - c[j]) / xrange[j];
+            acc += d * d;
+        }
+        unsigned int was_inside = inside;
+        inside = sqrt(acc) < op.nHoodRadius;
+        return was_inside && !inside;
+    }
+    __device__ __forceinline__ bool on_event(CLODE_HOOK_ARGS)
+    {
+        ++events;
+        if (events > 1) {
+            npk.push((realtype)peaks_now, events - 1);
+            period.push(t - t_last_event, events - 1);
+        }
+        t_last_event = t;
+        peaks_now = 0;
+        if (events <= N_STORE_EVENTS)
+            put(tex_list, events - 1, t);
+        return events == op.maxEventCount;
+    }
+    __device__ __forceinline__ void write(FOut &o) const
+    {
+        bool two = events > 1;
+        o(two ? period.hi : ZERO); o(two ? period.lo : ZERO); o(two ? period.mean : ZERO);
+        o(two ? npk.hi : ZERO); o(two ? npk.lo : ZERO); o(two ? npk.mean : ZERO);
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xmean[j]); o(xrange[j]); o(c[j]);
+            o(ext.dxmax[j]); o(ext.dxmin[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_AUX; ++j) {
+            o(ext.amax[j]); o(ext.amin[j]); o(ext.amean[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_STORE_EVENTS; ++j)
+            o(tex_list[j]);
+        o((realtype)events);
+        o((realtype)steps);
+        o(hstat.hi); o(hstat.lo); o(hstat.mean);
+    }
+    __device__ __forceinline__ void rebase(realtype T)
+    {
+        t_start -= T;
+        t_last_event -= T;
+        b.rebase(T);
+    }
+};
+
+#elif defined(USE_OBSERVER_THRESHOLD_2)
+#define CLODE_HAVE_OBSERVER 1
+struct Observer {
+    static constexpr bool two_pass = true;
+    SolBuf b;
+    Extent ext;
+    realtype tup_list[NSE1], tdown_list[NSE1];
+    Stat3 npk, period, updur, downdur, duty, dip, hstat;
+    realtype down_mean;
+    realtype gxmax, gxmin, gdxmax, gdxmin, x_up, x_down, dx_up, dx_down;
+    realtype t_start, t_last_event, t_down, t_last_max, t_last_min, x_last_min;
+    unsigned int peaks_now, steps, events, is_up;
+
+    __device__ __forceinline__ void init(CLODE_HOOK_ARGS)
+    {
+        b.seed(t, x, dx);
+        ext.reset();
+#pragma unroll
+        for (int j = 0; j < NSE1; ++j)
+            tup_list[j] = tdown_list[j] = ZERO;
+        npk.reset(); period.reset(); updur.reset(); downdur.reset(); duty.reset(); dip.reset(); hstat.reset();
+        down_mean = ZERO;
+        gxmax = -BIG_REAL; gxmin = BIG_REAL; gdxmax = -BIG_REAL; gdxmin = BIG_REAL;
+        x_up = ZERO; x_down = ZERO; dx_up = ZERO; dx_down = ZERO;
+        t_start = t; t_last_event = ZERO; t_down = ZERO; t_last_max = ZERO; t_last_min = ZERO;
+        x_last_min = BIG_REAL;
+        is_up = 0; peaks_now = 0; steps = 0; events = 0;
+    }
+    // first pass: extent of the event variable and of its slope
+    __device__ __forceinline__ void warmup(CLODE_HOOK_ARGS)
+    {
+        realtype xe = sel(x, op.eVarIx), de = sel(dx, op.eVarIx);
+        gxmax = fmax(gxmax, xe);
+        gxmin = fmin(gxmin, xe);
+        gdxmax = fmax(gdxmax, de);
+        gdxmin = fmin(gdxmin, de);
+    }
+    __device__ __forceinline__ void arm(CLODE_HOOK_ARGS)
+    {
+        realtype amp = gxmax - gxmin;
+        x_up = gxmin + op.xUpThresh * amp;
+        x_down = op.xDownThresh > ZERO ? gxmin + op.xDownThresh * amp : x_up;
+        dx_up = op.dxUpThresh * gdxmax;
+        dx_down = op.dxDownThresh > ZERO ? op.dxDownThresh * gdxmin : gdxmin;
+        is_up = sel(x, op.eVarIx) > x_up ? 1 : 0;
+    }
+    __device__ __forceinline__ void update(CLODE_HOOK_ARGS)
+    {
+        ++steps;
+        b.shift(t, x, dx);
+        realtype h = b.t2 - b.t1;
+        hstat.push(h, steps);
+        ext.update(x, dx, aux, h, t - t_start);
+        if (steps > 1) {
+            const unsigned int f = op.fVarIx, e = op.eVarIx;
+            realtype a0 = sel(b.x0, f), a1 = sel(b.x1, f), a2 = sel(b.x2, f);
+            realtype df1 = sel(b.d1, f), df2 = sel(b.d2, f);
+            if (df1 > ZERO && df2 < ZERO) {
+                int ix = argmax3(a0, a1, a2);
+                peaks_now++;
+                t_last_max = pick3(ix, b.t0, b.t1, b.t2);
+            }
+            if (df1 < ZERO && df2 > ZERO) {
+                int ix = argmin3(a0, a1, a2);
+                x_last_min = pick3(ix, a0, a1, a2);
+                t_last_min = pick3(ix, b.t0, b.t1, b.t2);
+            }
+            if (is_up) {
+                if (sel(x, e) <= x_down && sel(dx, e) >= dx_down) {
+                    t_down = t;
+                    is_up = 0;
+                    if (events > 0 && events <= N_STORE_EVENTS)
+                        put(tdown_list, events - 1, t_down);
+                    down_mean = sel(x, f);
+                }
+            } else {
+                realtype since_down = t - t_down;
+                if (since_down > ZERO)
+                    down_mean = mean_time(down_mean, sel(x, f), h, since_down);
+            }
+        }
+    }
+    __device__ __forceinline__ bool event(CLODE_HOOK_ARGS)
+    {
+        if (steps < 2)
+            return false;
+        if (gxmax - gxmin < op.minXamp)
+            return false;
+        if (is_up)
+            return false;
+        return sel(x, op.eVarIx) > x_up && sel(dx, op.eVarIx) > dx_up;
+    }
+    __device__ __forceinline__ bool on_event(CLODE_HOOK_ARGS)
+    {
+        ++events;
+        is_up = 1;
+        if (events > 1) {
+            unsigned int n = events - 1;
+            npk.push((realtype)peaks_now, n);
+            realtype per = t - t_last_event;
+            period.push(per, n);
+            realtype up = t_down - t_last_event;
+            updur.push(up, n);
+            downdur.push(t - t_down, n);
+            duty.push(up / per, n);
+            dip.push(down_mean - x_last_min, n);
+        }
+        if (events <= N_STORE_EVENTS)
+            put(tup_list, events - 1, t);
+        t_last_event = t;
+        peaks_now = 0;
+        return events == op.maxEventCount;
+    }
+    __device__ __forceinline__ void write(FOut &o) const
+    {
+        bool two = events > 1;
+        o(two ? period.hi : ZERO); o(two ? period.lo : ZERO); o(two ? period.mean : ZERO);
+        o(two ? npk.hi : ZERO); o(two ? npk.lo : ZERO); o(two ? npk.mean : ZERO);
+        o(two ? updur.hi : ZERO); o(two ? updur.lo : ZERO); o(two ? updur.mean : ZERO);
+        o(two ? downdur.hi : ZERO); o(two ? downdur.lo : ZERO); o(two ? downdur.mean : ZERO);
+        o(two ? duty.hi : ZERO); o(two ? duty.lo : ZERO); o(two ? duty.mean : ZERO);
+        o(two ? dip.hi : ZERO); o(two ? dip.lo : ZERO); o(two ? dip.mean : ZERO);
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xmean[j]); o(ext.dxmax[j]); o(ext.dxmin[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_AUX; ++j) {
+            o(ext.amax[j]); o(ext.amin[j]); o(ext.amean[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N_STORE_EVENTS; ++j) {
+            o(tup_list[j]); o(tdown_list[j]);
+        }
+        o((realtype)events);
+        o((realtype)steps);
+        o(hstat.hi); o(hstat.lo); o(hstat.mean);
+    }
+    __device__ __forceinline__ void rebase(realtype T)
+    {
+        t_start -= T;
+        t_last_event -= T;
+        t_down -= T;
+        t_last_max -= T;
+        t_last_min -= T;
+        b.rebase(T);
+    }
+};
+#else
+#define CLODE_HAVE_OBSERVER 0
+#endif
+
+}  // namespace clode

@@ -1,0 +1,283 @@
+// Time steppers.  Each member's state lives in registers (N_VAR, N_PAR, ...
+// are compile-time constants, so every array below is fully unrolled).
+//
+// Arithmetic follows the reference operation by operation, so that with
+// --fmad=false the results are bitwise those of clODE's kernels:
+//   Euler / stochastic Euler  clode/cpp/steppers/fixed_explicit_Euler.clh:5-18
+//   Heun                      clode/cpp/steppers/fixed_explicit_Trapezoidal.clh:5-23
+//   RK4                       clode/cpp/steppers/fixed_explicit_RK4.clh:5-40
+//   fixed-step wrapper        clode/cpp/steppers/fixed_explicit_step.clh:9-37
+//   BS23                      clode/cpp/steppers/adaptive_bs23.clh:27-63
+//   Dormand-Prince 5(4)       clode/cpp/steppers/adaptive_dp45.clh:10-111
+//   step-size controller      clode/cpp/steppers/adaptive_explicit_step.clh:4-81
+// Tableau entries are written as the same quotients the reference's macros
+// expand to; the compiler rounds each quotient once to working precision.
+#pragma once
+
+namespace clode {
+
+#define NP1 (N_PAR > 0 ? N_PAR : 1)
+#define NA1 (N_AUX > 0 ? N_AUX : 1)
+#define NW1 (N_WIENER > 0 ? N_WIENER : 1)
+
+#if defined(STOCHASTIC_EULER)
+#define CLODE_STOCHASTIC 1
+#else
+#define CLODE_STOCHASTIC 0
+#endif
+
+struct Member {
+    realtype t, dt;
+    realtype p[NP1];
+    realtype x[N_VAR];
+    realtype dx[N_VAR];
+    realtype aux[NA1];
+    realtype w[NW1];
+    Rng r;
+};
+
+// per-thread work counters, summed into ArgsT::stats at the end of a member
+struct Counters {
+    unsigned int steps, rejected, rhs, events;
+};
+
+typedef SolverParamsT<realtype> SolverParams;
+
+#if defined(EXPLICIT_EULER) || defined(STOCHASTIC_EULER) || defined(EXPLICIT_HEUN) || defined(EXPLICIT_RK4)
+#define CLODE_FIXED_STEP 1
+
+#if defined(EXPLICIT_EULER) || defined(STOCHASTIC_EULER)
+#define CLODE_RHS_PER_STEP 1
+#elif defined(EXPLICIT_HEUN)
+#define CLODE_RHS_PER_STEP 2
+#else
+#define CLODE_RHS_PER_STEP 4
+#endif
+
+__device__ __forceinline__ void fixed_do_step(realtype &t, realtype (&x)[N_VAR], const realtype (&k1)[N_VAR],
+                                              const realtype (&p)[NP1], const realtype dt, realtype (&aux)[NA1],
+                                              const realtype (&w)[NW1])
+{
+#if defined(EXPLICIT_EULER) || defined(STOCHASTIC_EULER)
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        x[k] += dt * k1[k];
+    t += dt;
+#elif defined(EXPLICIT_HEUN)
+    realtype tn = t + dt;
+    realtype xp[N_VAR], k2[N_VAR];
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xp[k] = fma(dt, k1[k], x[k]);
+    getRHS(tn, xp, p, k2, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        x[k] += dt * RCONST(0.5) * (k1[k] + k2[k]);
+    t = tn;
+#else
+    realtype xs[N_VAR], k2[N_VAR], k3[N_VAR], k4[N_VAR];
+    realtype half = dt * RCONST(0.5);
+    realtype tm = t + half;
+    realtype te = t + dt;
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + half * k1[k];
+    getRHS(tm, xs, p, k2, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + half * k2[k];
+    getRHS(tm, xs, p, k3, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + dt * k3[k];
+    getRHS(te, xs, p, k4, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        x[k] += dt * (k1[k] + RCONST(2.0) * k2[k] + RCONST(2.0) * k3[k] + k4[k]) / RCONST(6.0);
+    t = te;
+#endif
+}
+
+// one fixed step; afterwards m.dx holds f(t_new, x_new) with fresh noise
+__device__ __forceinline__ int step_member(Member &m, const SolverParams &sp, const realtype t1, Counters &c)
+{
+    fixed_do_step(m.t, m.x, m.dx, m.p, m.dt, m.aux, m.w);
+#if CLODE_STOCHASTIC
+#pragma unroll
+    for (int j = 0; j < N_WIENER; ++j)
+        m.w[j] = rng_normal(m.r) / sqrt(m.dt);
+#endif
+    getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
+    c.steps++;
+    c.rhs += CLODE_RHS_PER_STEP;
+    return 0;
+}
+
+#elif defined(EXPLICIT_BS23) || defined(EXPLICIT_DOPRI5)
+#define CLODE_FIXED_STEP 0
+
+#if defined(EXPLICIT_BS23)
+#define CLODE_ERR_ORDER RCONST(2.0)
+#define CLODE_MAX_SHRINK RCONST(0.5)
+#define CLODE_MAX_GROW RCONST(5.0)
+#define CLODE_RHS_PER_ATTEMPT 3
+
+// returns the effective step tnew - t; x, k1 (FSAL) and t advance in place
+__device__ __forceinline__ realtype attempt(realtype &t, realtype (&x)[N_VAR], realtype (&k1)[N_VAR],
+                                            const realtype (&p)[NP1], const realtype dt, realtype (&aux)[NA1],
+                                            realtype (&err)[N_VAR], const realtype (&w)[NW1])
+{
+    const realtype b1 = RCONST(2.0) / RCONST(9.0), b2 = RCONST(1.0) / RCONST(3.0), b3 = RCONST(4.0) / RCONST(9.0);
+    const realtype e1 = RCONST(-5.0) / RCONST(72.0), e2 = RCONST(1.0) / RCONST(12.0);
+    const realtype e3 = RCONST(1.0) / RCONST(9.0), e4 = RCONST(-1.0) / RCONST(8.0);
+    realtype tn = t + dt;
+    realtype h = tn - t;
+    realtype xs[N_VAR], k2[N_VAR], k3[N_VAR], k4[N_VAR];
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + h * RCONST(0.5) * k1[k];
+    getRHS(t + h * RCONST(0.5), xs, p, k2, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + h * RCONST(0.75) * k2[k];
+    getRHS(t + h * RCONST(0.75), xs, p, k3, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        x[k] = x[k] + h * (b1 * k1[k] + b2 * k2[k] + b3 * k3[k]);
+    getRHS(tn, x, p, k4, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k) {
+        err[k] = h * (e1 * k1[k] + e2 * k2[k] + e3 * k3[k] + e4 * k4[k]);
+        k1[k] = k4[k];
+    }
+    t = tn;
+    return h;
+}
+#else
+#define CLODE_ERR_ORDER RCONST(4.0)
+#define CLODE_MAX_SHRINK RCONST(0.1)
+#define CLODE_MAX_GROW RCONST(5.0)
+#define CLODE_RHS_PER_ATTEMPT 6
+
+__device__ __forceinline__ realtype attempt(realtype &t, realtype (&x)[N_VAR], realtype (&k1)[N_VAR],
+                                            const realtype (&p)[NP1], const realtype dt, realtype (&aux)[NA1],
+                                            realtype (&err)[N_VAR], const realtype (&w)[NW1])
+{
+    const realtype a2 = RCONST(1.0) / RCONST(5.0), a3 = RCONST(3.0) / RCONST(10.0);
+    const realtype a4 = RCONST(4.0) / RCONST(5.0), a5 = RCONST(8.0) / RCONST(9.0);
+    const realtype b21 = RCONST(1.0) / RCONST(5.0);
+    const realtype b31 = RCONST(3.0) / RCONST(40.0), b32 = RCONST(9.0) / RCONST(40.0);
+    const realtype b41 = RCONST(44.0) / RCONST(45.0), b42 = RCONST(-56.0) / RCONST(15.0);
+    const realtype b43 = RCONST(32.0) / RCONST(9.0);
+    const realtype b51 = RCONST(19372.0) / RCONST(6561.0), b52 = RCONST(-25360.0) / RCONST(2187.0);
+    const realtype b53 = RCONST(64448.0) / RCONST(6561.0), b54 = RCONST(-212.0) / RCONST(729.0);
+    const realtype b61 = RCONST(9017.0) / RCONST(3168.0), b62 = RCONST(-355.0) / RCONST(33.0);
+    const realtype b63 = RCONST(46732.0) / RCONST(5247.0), b64 = RCONST(49.0) / RCONST(176.0);
+    const realtype b65 = RCONST(-5103.0) / RCONST(18656.0);
+    const realtype c1 = RCONST(35.0) / RCONST(384.0), c3 = RCONST(500.0) / RCONST(1113.0);
+    const realtype c4 = RCONST(125.0) / RCONST(192.0), c5 = RCONST(-2187.0) / RCONST(6784.0);
+    const realtype c6 = RCONST(11.0) / RCONST(84.0);
+    const realtype e1 = RCONST(71.0) / RCONST(57600.0), e3 = RCONST(-71.0) / RCONST(16695.0);
+    const realtype e4 = RCONST(71.0) / RCONST(1920.0), e5 = RCONST(-17253.0) / RCONST(339200.0);
+    const realtype e6 = RCONST(22.0) / RCONST(525.0), e7 = RCONST(-1.0) / RCONST(40.0);
+
+    realtype tn = t + dt;
+    realtype h = tn - t;
+    realtype xs[N_VAR], k2[N_VAR], k3[N_VAR], k4[N_VAR], k5[N_VAR], k6[N_VAR], k7[N_VAR];
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + h * (b21 * k1[k]);
+    getRHS(t + a2 * h, xs, p, k2, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + h * (b31 * k1[k] + b32 * k2[k]);
+    getRHS(t + a3 * h, xs, p, k3, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + h * (b41 * k1[k] + b42 * k2[k] + b43 * k3[k]);
+    getRHS(t + a4 * h, xs, p, k4, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + h * (b51 * k1[k] + b52 * k2[k] + b53 * k3[k] + b54 * k4[k]);
+    getRHS(t + a5 * h, xs, p, k5, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        xs[k] = x[k] + h * (b61 * k1[k] + b62 * k2[k] + b63 * k3[k] + b64 * k4[k] + b65 * k5[k]);
+    getRHS(t + h, xs, p, k6, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k)
+        x[k] = x[k] + h * (c1 * k1[k] + c3 * k3[k] + c4 * k4[k] + c5 * k5[k] + c6 * k6[k]);
+    getRHS(tn, x, p, k7, aux, w);
+#pragma unroll
+    for (int k = 0; k < N_VAR; ++k) {
+        err[k] = h * (e1 * k1[k] + e3 * k3[k] + e4 * k4[k] + e5 * k5[k] + e6 * k6[k] + e7 * k7[k]);
+        k1[k] = k7[k];
+    }
+    t = tn;
+    return h;
+}
+#endif
+
+// adaptive step with error control; returns -1 when the step fails at hmin
+// (the reference ignores that flag and keeps stepping; the caller records it)
+__device__ __forceinline__ int step_member(Member &m, const SolverParams &sp, const realtype t1, Counters &c)
+{
+    const realtype safety = RCONST(0.8);
+    const realtype expon = RCONST(1.0) / (CLODE_ERR_ORDER + RCONST(1.0));
+    realtype tn, nerr = ZERO;
+    realtype err[N_VAR], xn[N_VAR], kn[N_VAR];
+    realtype h = m.dt;
+    const realtype threshold = sp.abstol / sp.reltol;
+    const realtype hmin = RCONST(16.0) * fabs(fabs(nextafter(m.t, RCONST(1.1) * t1)) - m.t);
+    bool first_try = true;
+    for (;;) {
+        tn = m.t;
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            xn[j] = m.x[j];
+            kn[j] = m.dx[j];
+        }
+        h = clamp(h, hmin, sp.dtmax);
+        h = attempt(tn, xn, kn, m.p, h, m.aux, err, m.w);
+        c.rhs += CLODE_RHS_PER_ATTEMPT;
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            err[j] /= fmax(fmax(fabs(m.x[j]), fabs(xn[j])), threshold);
+        nerr = ZERO;
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            nerr = fmax(fabs(err[j]), nerr);
+        if (!(nerr > sp.reltol))
+            break;
+        c.rejected++;
+        if (h <= hmin) {
+            m.dt = hmin;
+            c.steps++;
+            return -1;
+        }
+        if (first_try) {
+            first_try = false;
+            h *= fmax(CLODE_MAX_SHRINK, safety * pow(sp.reltol / nerr, expon));
+        } else {
+            h *= RCONST(0.5);
+        }
+    }
+    if (first_try)
+        h *= fmin(CLODE_MAX_GROW, safety * pow(sp.reltol / nerr, expon));
+    h = fmin(h, t1 - tn);
+    h = clamp(h, hmin, sp.dtmax);
+    m.dt = h;
+    m.t = tn;
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j) {
+        m.x[j] = xn[j];
+        m.dx[j] = kn[j];
+    }
+    c.steps++;
+    return 0;
+}
+#else
+#error "no stepper selected: define one of EXPLICIT_EULER, EXPLICIT_HEUN, EXPLICIT_RK4, EXPLICIT_BS23, EXPLICIT_DOPRI5, STOCHASTIC_EULER"
+#endif
+
+}  // namespace clode

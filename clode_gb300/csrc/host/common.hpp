@@ -1,0 +1,71 @@
+// Internal declarations shared by the host runtime translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../../include/clode_gb300.h"
+
+namespace clode {
+
+// An error carrying a CLODE_ERR_* code; the C ABI converts it to a status.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &msg) : std::runtime_error(msg), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const char *fmt, ...);
+void check_cuda(cudaError_t e, const char *what);
+
+// ------------------------------------------------------------------ logging
+// A process-wide logger with the levels of clODE's LogLevel enum; messages go
+// to stdout, or to a sink installed with clode_log_set_sink().
+void log_msg(int level, const char *fmt, ...);
+int log_level();
+
+// ----------------------------------------------------------------- devices
+// Makes `device` current on this thread (and initialises its primary context).
+void use_device(int device);
+int device_count_or_zero();
+
+// ------------------------------------------------------------ NVRTC programs
+struct ProgramSpec {
+    std::string rhs_source;
+    std::string rhs_name;
+    std::vector<std::string> defines;   // "-DNAME=VALUE"
+    bool fmad = false;
+    std::string arch;                   // e.g. "sm_103a"
+};
+
+struct CompiledProgram {
+    std::vector<char> cubin;
+    std::string log;
+    std::string source;                 // the full program text handed to NVRTC
+    std::string options;
+    std::string key;
+};
+
+// Compile (or fetch from the on-disk cache) the ensemble program for `spec`.
+CompiledProgram compile_program(const ProgramSpec &spec);
+// "sm_XY[a]" of a device; "sm_103a" when no device is present.
+std::string device_arch(int device);
+void set_cache_dir(const std::string &dir);
+
+// every kernel launch the library issues is counted (clode_launch_count)
+void count_launch();
+
+// -------------------------------------------------------------- AOT kernels
+void launch_f64_to_f32(const double *src, float *dst, size_t n, cudaStream_t s);
+void launch_f32_to_f64(const float *src, double *dst, size_t n, cudaStream_t s);
+void launch_seed_rng_sequential(unsigned long long *rng, size_t n, int seed, cudaStream_t s);
+void launch_seed_rng_random(unsigned long long *rng, size_t n, unsigned long long base, cudaStream_t s);
+void launch_fill_f32(float *dst, float v, size_t n, cudaStream_t s);
+void launch_fill_f64(double *dst, double v, size_t n, cudaStream_t s);
+void launch_fill_i32(int *dst, int v, size_t n, cudaStream_t s);
+
+}  // namespace clode

@@ -1,0 +1,1278 @@
+// The simulator object behind the C ABI: one ensemble problem, its device
+// buffers, its compiled program and its CUDA stream.  It re-implements the
+// host logic of clODE's CLODE, CLODEfeatures and CLODEtrajectory classes
+// (clode/cpp/CLODE.cpp, CLODEfeatures.cpp, CLODEtrajectory.cpp) over CUDA:
+// buffer sizing on nPts changes, precision conversion of host doubles,
+// RNG seeding, dt persistence for adaptive continuation, lazy observer
+// initialisation and the x0/tspan shifts for continuation runs.
+#include "common.hpp"
+#include "../device/clode_args.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <random>
+#include <sstream>
+
+using namespace clode;
+
+namespace {
+
+// stepper name -> define (clode/cpp/steppers.cl:26-43)
+const std::map<std::string, std::string> kSteppers = {
+    {"euler", "EXPLICIT_EULER"}, {"heun", "EXPLICIT_HEUN"},     {"rk4", "EXPLICIT_RK4"},
+    {"bs23", "EXPLICIT_BS23"},   {"dopri5", "EXPLICIT_DOPRI5"}, {"seuler", "STOCHASTIC_EULER"},
+};
+
+// observer name -> define (clode/cpp/observers.cl:122-143)
+const std::map<std::string, std::string> kObservers = {
+    {"basic", "USE_OBSERVER_BASIC"},
+    {"basicall", "USE_OBSERVER_BASIC_ALLVAR"},
+    {"localmax", "USE_OBSERVER_LOCAL_MAX"},
+    {"nhood1", "USE_OBSERVER_NEIGHBORHOOD_1"},
+    {"nhood2", "USE_OBSERVER_NEIGHBORHOOD_2"},
+    {"thresh2", "USE_OBSERVER_THRESHOLD_2"},
+};
+
+std::vector<std::string> split_lines(const char *s)
+{
+    std::vector<std::string> out;
+    if (!s)
+        return out;
+    std::string cur;
+    for (const char *p = s; *p; ++p) {
+        if (*p == '\n') {
+            out.push_back(cur);
+            cur.clear();
+        } else {
+            cur += *p;
+        }
+    }
+    if (!cur.empty())
+        out.push_back(cur);
+    return out;
+}
+
+// Feature names, in the order the kernels write F: the getObserverInfo_*
+// lists of clode/cpp/observers/observer_*.clh
+std::vector<std::string> feature_names(const std::string &obs, const std::vector<std::string> &vars,
+                                       const std::vector<std::string> &auxs, unsigned int fvar, unsigned int nse)
+{
+    std::vector<std::string> f;
+    auto extent = [&](bool with_range_centre) {
+        for (auto &v : vars) {
+            f.push_back("max " + v);
+            f.push_back("min " + v);
+            f.push_back("mean " + v);
+            if (with_range_centre) {
+                f.push_back("range " + v);
+                f.push_back("nhood center " + v);
+            }
+            f.push_back("max d" + v + "/dt");
+            f.push_back("min d" + v + "/dt");
+        }
+        for (auto &a : auxs) {
+            f.push_back("max " + a);
+            f.push_back("min " + a);
+            f.push_back("mean " + a);
+        }
+    };
+    if (obs == "basic") {
+        std::string v = fvar < vars.size() ? vars[fvar] : std::string("");
+        f = {"max " + v, "min " + v, "mean " + v, "max d" + v + "/dt", "min d" + v + "/dt", "step count"};
+    } else if (obs == "basicall") {
+        extent(false);
+        f.push_back("step count");
+    } else if (obs == "localmax") {
+        f = {"max IMI", "min IMI", "mean IMI", "max amplitude", "min amplitude", "mean amplitude"};
+        extent(false);
+        for (unsigned j = 0; j < nse; ++j) {
+            f.push_back("localmax event time " + std::to_string(j));
+            f.push_back("localmax event evar " + std::to_string(j));
+            f.push_back("localmin event time " + std::to_string(j));
+            f.push_back("localmin event evar " + std::to_string(j));
+        }
+        f.push_back("event count");
+        f.push_back("step count");
+    } else if (obs == "nhood1") {
+        f = {"max period", "min period", "mean period", "max peaks", "min peaks", "mean peaks"};
+        extent(false);
+        f.push_back("period count");
+        f.push_back("step count");
+        f.push_back("max dt");
+        f.push_back("min dt");
+        f.push_back("mean dt");
+    } else if (obs == "nhood2") {
+        f = {"max period", "min period", "mean period", "max peaks", "min peaks", "mean peaks"};
+        extent(true);
+        for (unsigned j = 0; j < nse; ++j)
+            f.push_back("nhood event time " + std::to_string(j));
+        f.push_back("event count");
+        f.push_back("step count");
+        f.push_back("max dt");
+        f.push_back("min dt");
+        f.push_back("mean dt");
+    } else if (obs == "thresh2") {
+        for (const char *g : {"period", "peaks", "upDuration", "downDuration", "duty", "activeDip"}) {
+            f.push_back(std::string("max ") + g);
+            f.push_back(std::string("min ") + g);
+            f.push_back(std::string("mean ") + g);
+        }
+        extent(false);
+        for (unsigned j = 0; j < nse; ++j) {
+            f.push_back("up event time " + std::to_string(j));
+            f.push_back("down event time " + std::to_string(j));
+        }
+        f.push_back("event count");
+        f.push_back("step count");
+        f.push_back("max dt");
+        f.push_back("min dt");
+        f.push_back("mean dt");
+    }
+    return f;
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    void reserve(size_t b)
+    {
+        if (b <= bytes && p)
+            return;
+        release();
+        if (b == 0)
+            return;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            bytes = 0;
+            cudaGetLastError();
+            fail(CLODE_ERR_OUT_OF_MEMORY, "cannot allocate %.3f GB on the device: %s", b / 1e9, cudaGetErrorString(e));
+        }
+        bytes = b;
+    }
+    void release()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T *as() const { return (T *)p; }
+};
+
+thread_local std::string g_last_error;
+
+}  // namespace
+
+struct clode_sim {
+    int kind = CLODE_SIM_BASE;
+    // problem (ProblemInfo)
+    std::string rhs_source, rhs_name;
+    int nVar = 0, nPar = 0, nAux = 0, nWiener = 0;
+    std::vector<std::string> var_names, par_names, aux_names;
+    std::string stepper, observer;
+    bool single = true;
+    int device = 0;
+    clode_solver_params sp = {0.1, 0.5, 1e-6, 1e-3, 1000000u, 1000000u, 1u};
+    clode_observer_params op = {0u, 0u, 100u, 0u, 0.0, 0.0, 0.05, 0.2, 0.2, 0.0, 0.0, 0.0};
+    double tspan[2] = {0.0, 1000.0};
+    bool tspan_per_member = false;
+    std::vector<double> tspan_pm;
+    long long nPts = 0;
+    std::vector<double> pars_host;
+
+    // device state
+    int buffers_device = -1;
+    bool buffers_single = true;
+    DevBuf x0, pars, xf, rng, dt, tf, tspan_dev, odata, F, t, x, dx, aux, nstored, status, stats, stage, work;
+
+    // program
+    bool built = false;
+    CompiledProgram prog;
+    std::string built_key;
+    cudaLibrary_t lib = nullptr;
+    int lib_device = -1;
+    cudaKernel_t k_transient = nullptr, k_trajectory = nullptr, k_init = nullptr, k_features = nullptr;
+    unsigned int obs_words = 0;
+    unsigned int built_nse = 0;
+
+    // features bookkeeping (CLODEfeatures.cpp:143-177)
+    long long F_elements = -1;
+    unsigned int odata_words_alloc = 0;
+    bool observer_initialized = false;
+    // trajectory bookkeeping (CLODEtrajectory.cpp:45-94)
+    long long traj_rows = -1, traj_pts = -1;
+
+    // engine options
+    int schedule = 0;
+    int block_size = 128;
+    int blocks_per_sm = 0;
+    bool fmad = false;
+    double time_budget_ms = 0.0;
+    bool fuse_init = true;
+    bool collect_stats = true;
+
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
+    unsigned long long last_stats[CLODE_STAT_COUNT] = {0};
+
+    ~clode_sim()
+    {
+        if (buffers_device >= 0 || lib) {
+            cudaSetDevice(buffers_device >= 0 ? buffers_device : lib_device);
+            for (DevBuf *b : all_buffers())
+                b->release();
+            if (lib)
+                cudaLibraryUnload(lib);
+            if (stream)
+                cudaStreamDestroy(stream);
+            if (ev0)
+                cudaEventDestroy(ev0);
+            if (ev1)
+                cudaEventDestroy(ev1);
+        }
+    }
+
+    std::vector<DevBuf *> all_buffers()
+    {
+        return {&x0, &pars, &xf, &rng, &dt, &tf, &tspan_dev, &odata, &F, &t, &x, &dx, &aux, &nstored, &status, &stats, &stage, &work};
+    }
+
+    size_t real_size() const { return single ? sizeof(float) : sizeof(double); }
+
+    // --------------------------------------------------------- set-up --
+    void set_problem(const clode_problem *p)
+    {
+        if (!p || !p->rhs_source)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "problem info with an RHS source is required");
+        if (p->n_var < 1 || p->n_par < 0 || p->n_aux < 0 || p->n_wiener < 0)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "invalid problem sizes nVar=%d nPar=%d nAux=%d nWiener=%d", p->n_var,
+                 p->n_par, p->n_aux, p->n_wiener);
+        rhs_source = p->rhs_source;
+        rhs_name = p->rhs_name ? p->rhs_name : "rhs.cl";
+        nVar = p->n_var;
+        nPar = p->n_par;
+        nAux = p->n_aux;
+        nWiener = p->n_wiener;
+        var_names = split_lines(p->var_names);
+        par_names = split_lines(p->par_names);
+        aux_names = split_lines(p->aux_names);
+        while ((int)var_names.size() < nVar)
+            var_names.push_back("x" + std::to_string(var_names.size()));
+        while ((int)aux_names.size() < nAux)
+            aux_names.push_back("aux" + std::to_string(aux_names.size()));
+        var_names.resize(nVar);
+        aux_names.resize(nAux);
+        built = false;
+    }
+
+    void set_stepper(const char *s)
+    {
+        std::string n = s ? s : "";
+        if (kSteppers.count(n))
+            stepper = n;
+        else
+            log_msg(CLODE_LOG_WARN, "Unknown stepper: %s. Stepper method unchanged", n.c_str());
+        built = false;
+    }
+
+    void set_observer(const char *s)
+    {
+        std::string n = s ? s : "";
+        if (kObservers.count(n))
+            observer = n;
+        else
+            log_msg(CLODE_LOG_WARN, "unknown observer: %s. Observer method unchanged", n.c_str());
+        built = false;
+    }
+
+    std::vector<std::string> names() const
+    {
+        return feature_names(observer, var_names, aux_names, op.f_var_ix, op.max_event_timestamps);
+    }
+
+    void ensure_stream()
+    {
+        use_device(device);
+        if (!stream || buffers_device != device) {
+            if (stream && buffers_device >= 0) {
+                cudaSetDevice(buffers_device);
+                cudaStreamDestroy(stream);
+                cudaEventDestroy(ev0);
+                cudaEventDestroy(ev1);
+                cudaSetDevice(device);
+            }
+            check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            check_cuda(cudaEventCreate(&ev0), "cudaEventCreate");
+            check_cuda(cudaEventCreate(&ev1), "cudaEventCreate");
+        }
+    }
+
+    // ------------------------------------------------------------ build --
+    ProgramSpec spec() const
+    {
+        ProgramSpec s;
+        s.rhs_source = rhs_source;
+        s.rhs_name = rhs_name;
+        s.fmad = fmad;
+        s.arch = device_arch(device);
+        s.defines = {single ? "-DCLODE_SINGLE_PRECISION" : "-DCLODE_DOUBLE_PRECISION", "-D" + kSteppers.at(stepper),
+                     "-DN_PAR=" + std::to_string(nPar), "-DN_VAR=" + std::to_string(nVar),
+                     "-DN_AUX=" + std::to_string(nAux), "-DN_WIENER=" + std::to_string(nWiener)};
+        if (kind == CLODE_SIM_FEATURES) {
+            s.defines.push_back("-D" + kObservers.at(observer));
+            s.defines.push_back("-DN_STORE_EVENTS=" + std::to_string(op.max_event_timestamps));
+        } else {
+            s.defines.push_back("-DN_STORE_EVENTS=0");
+        }
+        return s;
+    }
+
+    void build()
+    {
+        if (rhs_source.empty())
+            fail(CLODE_ERR_STATE, "no problem info set");
+        if (!kSteppers.count(stepper))
+            fail(CLODE_ERR_INVALID_ARGUMENT, "no valid stepper selected");
+        if (kind == CLODE_SIM_FEATURES && !kObservers.count(observer))
+            fail(CLODE_ERR_INVALID_ARGUMENT, "no valid observer selected");
+        if (kind == CLODE_SIM_FEATURES && nVar > 0 && (op.e_var_ix >= (unsigned)nVar || op.f_var_ix >= (unsigned)nVar))
+            fail(CLODE_ERR_INVALID_ARGUMENT, "observer variable index out of range (eVarIx=%u fVarIx=%u nVar=%d)",
+                 op.e_var_ix, op.f_var_ix, nVar);
+        ProgramSpec s = spec();
+        CompiledProgram p = compile_program(s);
+        bool have_device = device_count_or_zero() > 0;
+        if (have_device) {
+            use_device(device);
+            cudaLibrary_t nl = nullptr;
+            check_cuda(cudaLibraryLoadData(&nl, p.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
+                       "loading the ensemble program");
+            if (lib) {
+                cudaSetDevice(lib_device);
+                cudaLibraryUnload(lib);
+                cudaSetDevice(device);
+            }
+            lib = nl;
+            lib_device = device;
+            check_cuda(cudaLibraryGetKernel(&k_transient, lib, "clode_transient"), "kernel clode_transient");
+            check_cuda(cudaLibraryGetKernel(&k_trajectory, lib, "clode_trajectory"), "kernel clode_trajectory");
+            k_init = k_features = nullptr;
+            obs_words = 0;
+            if (kind == CLODE_SIM_FEATURES) {
+                check_cuda(cudaLibraryGetKernel(&k_init, lib, "clode_init_observer"), "kernel clode_init_observer");
+                check_cuda(cudaLibraryGetKernel(&k_features, lib, "clode_features"), "kernel clode_features");
+                void *gp = nullptr;
+                size_t gb = 0;
+                check_cuda(cudaLibraryGetGlobal(&gp, &gb, lib, "clode_observer_words"), "observer state size");
+                check_cuda(cudaMemcpy(&obs_words, gp, sizeof obs_words, cudaMemcpyDeviceToHost), "observer state size");
+            }
+        }
+        prog = p;
+        built_key = p.key;
+        built_nse = op.max_event_timestamps;
+        built = true;
+        log_msg(CLODE_LOG_DEBUG, "program %s ready (%s, %s, %s)", p.key.c_str(), stepper.c_str(),
+                kind == CLODE_SIM_FEATURES ? observer.c_str() : "-", single ? "single" : "double");
+    }
+
+    void ensure_built()
+    {
+        if (!built || lib == nullptr || lib_device != device ||
+            (kind == CLODE_SIM_FEATURES && built_nse != op.max_event_timestamps)) {
+            if (device_count_or_zero() == 0)
+                fail(CLODE_ERR_NO_DEVICE, "no CUDA device is available (this engine has no CPU path)");
+            build();
+        }
+    }
+
+    // ---------------------------------------------------- problem data --
+    void upload(DevBuf &dst, const double *src, size_t n)
+    {
+        if (n == 0)
+            return;
+        if (single) {
+            stage.reserve(n * sizeof(double));
+            check_cuda(cudaMemcpyAsync(stage.p, src, n * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D copy");
+            launch_f64_to_f32(stage.as<double>(), dst.as<float>(), n, stream);
+        } else {
+            check_cuda(cudaMemcpyAsync(dst.p, src, n * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D copy");
+        }
+        check_cuda(cudaStreamSynchronize(stream), "H2D copy");
+    }
+
+    void download(const DevBuf &src, double *dst, size_t n)
+    {
+        if (n == 0)
+            return;
+        if (single) {
+            stage.reserve(n * sizeof(double));
+            launch_f32_to_f64(src.as<float>(), stage.as<double>(), n, stream);
+            check_cuda(cudaMemcpyAsync(dst, stage.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H copy");
+        } else {
+            check_cuda(cudaMemcpyAsync(dst, src.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H copy");
+        }
+        check_cuda(cudaStreamSynchronize(stream), "D2H copy");
+    }
+
+    void fill_real(DevBuf &b, double v, size_t n)
+    {
+        if (single)
+            launch_fill_f32(b.as<float>(), (float)v, n, stream);
+        else
+            launch_fill_f64(b.as<double>(), v, n, stream);
+    }
+
+    // CLODE::setNpts (CLODE.cpp:174-242): resize, dt = sp.dt, random seed
+    void set_npts(long long n)
+    {
+        ensure_stream();
+        bool realloc = n != nPts || buffers_device != device || buffers_single != single;
+        if (!realloc)
+            return;
+        if (buffers_device >= 0 && buffers_device != device) {
+            cudaSetDevice(buffers_device);
+            for (DevBuf *b : all_buffers())
+                b->release();
+            cudaSetDevice(device);
+        }
+        nPts = n;
+        buffers_device = device;
+        buffers_single = single;
+        size_t rs = real_size();
+        x0.reserve(std::max<size_t>(1, nVar * n) * rs);
+        pars.reserve(std::max<size_t>(1, nPar * n) * rs);
+        xf.reserve(std::max<size_t>(1, nVar * n) * rs);
+        rng.reserve(std::max<size_t>(1, 2 * n) * sizeof(unsigned long long));
+        dt.reserve(std::max<size_t>(1, n) * rs);
+        tf.reserve(std::max<size_t>(1, n) * rs);
+        status.reserve(std::max<size_t>(1, n) * sizeof(int));
+        stats.reserve(CLODE_STAT_COUNT * sizeof(unsigned long long));
+        work.reserve(64);
+        fill_real(dt, sp.dt, n);
+        F_elements = -1;
+        traj_rows = -1;
+        observer_initialized = false;
+        if (tspan_per_member && (long long)tspan_pm.size() != 2 * n) {
+            tspan_per_member = false;
+            log_msg(CLODE_LOG_WARN, "ensemble size changed: per-member time spans dropped, using [%g, %g]", tspan[0],
+                    tspan[1]);
+        }
+        seed_rng(false, 0);
+        log_msg(CLODE_LOG_DEBUG, "set nPts=%lld", n);
+    }
+
+    void set_problem_data(const double *nx0, size_t n_x0, const double *np, size_t n_p)
+    {
+        if (n_x0 % (size_t)nVar != 0)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "Invalid initial condition vector: not a multiple of nVar=%d", nVar);
+        long long n = (long long)(n_x0 / nVar);
+        if (nPar > 0) {
+            if (n_p % (size_t)nPar != 0)
+                fail(CLODE_ERR_INVALID_ARGUMENT, "Invalid parameter vector: not a multiple of nPar=%d", nPar);
+            if ((long long)(n_p / nPar) != n)
+                fail(CLODE_ERR_INVALID_ARGUMENT,
+                     "Initial condition and parameter vector dimensions don't match: %lld sets of x0, %zu of pars", n,
+                     n_p / nPar);
+        } else if (n_p != 0) {
+            fail(CLODE_ERR_INVALID_ARGUMENT, "parameters given for a problem with nPar=0");
+        }
+        if (n > INT32_MAX / 2)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "nPts=%lld exceeds the supported maximum %d", n, INT32_MAX / 2);
+        set_npts(n);
+        set_x0(nx0, n_x0);
+        set_pars(np, n_p);
+    }
+
+    void set_x0(const double *v, size_t n)
+    {
+        if ((long long)n != nPts * nVar)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "Invalid initial condition vector: expected %lld*%d elements, received %zu",
+                 nPts, nVar, n);
+        ensure_stream();
+        upload(x0, v, n);
+    }
+
+    void set_pars(const double *v, size_t n)
+    {
+        if ((long long)n != nPts * nPar)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "Invalid parameter vector: expected %lld*%d elements, received %zu", nPts,
+                 nPar, n);
+        ensure_stream();
+        pars_host.assign(v, v + n);
+        upload(pars, v, n);
+    }
+
+    void seed_rng(bool use_seed, int seed)
+    {
+        if (nPts == 0)
+            return;
+        ensure_stream();
+        if (use_seed) {
+            launch_seed_rng_sequential(rng.as<unsigned long long>(), 2 * (size_t)nPts, seed, stream);
+        } else {
+            std::random_device rd;
+            unsigned long long base = ((unsigned long long)rd() << 32) ^ rd();
+            launch_seed_rng_random(rng.as<unsigned long long>(), 2 * (size_t)nPts, base, stream);
+        }
+        check_cuda(cudaStreamSynchronize(stream), "RNG seeding");
+    }
+
+    // ------------------------------------------------------------ runs --
+    template <typename R>
+    ArgsT<R> make_args()
+    {
+        ArgsT<R> a;
+        memset(&a, 0, sizeof a);
+        a.nPts = (int)nPts;
+        a.i_begin = 0;
+        a.i_end = (int)nPts;
+        a.t0 = (R)tspan[0];
+        a.t1 = (R)tspan[1];
+        a.tspan_pm = tspan_per_member ? tspan_dev.as<R>() : nullptr;
+        a.x0 = x0.as<R>();
+        a.pars = pars.as<R>();
+        a.xf = xf.as<R>();
+        a.rng = rng.as<unsigned long long>();
+        a.dt = dt.as<R>();
+        a.tf = tf.as<R>();
+        a.odata = odata.as<unsigned int>();
+        a.F = F.as<R>();
+        a.t_out = t.as<R>();
+        a.x_out = x.as<R>();
+        a.dx_out = dx.as<R>();
+        a.aux_out = aux.as<R>();
+        a.n_stored = nstored.as<int>();
+        a.status = status.as<int>();
+        a.stats = collect_stats ? stats.as<unsigned long long>() : nullptr;
+        a.work_next = work.as<unsigned int>();
+        a.time_budget_ns = (unsigned long long)(time_budget_ms * 1e6);
+        a.sp.dt = (R)sp.dt;
+        a.sp.dtmax = (R)sp.dtmax;
+        a.sp.abstol = (R)sp.abstol;
+        a.sp.reltol = (R)sp.reltol;
+        a.sp.max_steps = sp.max_steps;
+        a.sp.max_store = sp.max_store;
+        a.sp.nout = sp.nout;
+        a.op.eVarIx = op.e_var_ix;
+        a.op.fVarIx = op.f_var_ix;
+        a.op.maxEventCount = op.max_event_count;
+        a.op.maxEventTimestamps = op.max_event_timestamps;
+        a.op.minXamp = (R)op.min_x_amp;
+        a.op.minIMI = (R)op.min_imi;
+        a.op.nHoodRadius = (R)op.nhood_radius;
+        a.op.xUpThresh = (R)op.x_up_thresh;
+        a.op.xDownThresh = (R)op.x_down_thresh;
+        a.op.dxUpThresh = (R)op.dx_up_thresh;
+        a.op.dxDownThresh = (R)op.dx_down_thresh;
+        a.op.eps_dx = (R)op.eps_dx;
+        return a;
+    }
+
+    void launch(cudaKernel_t k, int fused_init)
+    {
+        if (nPts == 0)
+            return;
+        unsigned int block = (unsigned int)std::max(32, std::min(1024, block_size));
+        unsigned int grid = (unsigned int)((nPts + block - 1) / block);
+        if (single) {
+            ArgsT<float> a = make_args<float>();
+            a.fused_init = fused_init;
+            void *params[] = {&a};
+            check_cuda(cudaLaunchKernel((const void *)k, dim3(grid), dim3(block), params, 0, stream), "kernel launch");
+            count_launch();
+        } else {
+            ArgsT<double> a = make_args<double>();
+            a.fused_init = fused_init;
+            void *params[] = {&a};
+            check_cuda(cudaLaunchKernel((const void *)k, dim3(grid), dim3(block), params, 0, stream), "kernel launch");
+            count_launch();
+        }
+    }
+
+    void begin_run()
+    {
+        ensure_built();
+        ensure_stream();
+        if (collect_stats && nPts > 0)
+            check_cuda(cudaMemsetAsync(stats.p, 0, CLODE_STAT_COUNT * sizeof(unsigned long long), stream), "stats reset");
+        check_cuda(cudaEventRecord(ev0, stream), "event record");
+    }
+
+    void end_run(const char *what)
+    {
+        check_cuda(cudaEventRecord(ev1, stream), "event record");
+        check_cuda(cudaStreamSynchronize(stream), what);
+        float ms = 0.0f;
+        check_cuda(cudaEventElapsedTime(&ms, ev0, ev1), "event timing");
+        last_ms = ms;
+        memset(last_stats, 0, sizeof last_stats);
+        if (collect_stats && nPts > 0)
+            check_cuda(cudaMemcpy(last_stats, stats.p, sizeof last_stats, cudaMemcpyDeviceToHost), "stats read");
+    }
+
+    void require_problem()
+    {
+        if (buffers_device < 0)
+            fail(CLODE_ERR_STATE, "problem data must be set before running (set_problem_data)");
+    }
+
+    void sync_tspan_device()
+    {
+        if (!tspan_per_member)
+            return;
+        tspan_dev.reserve(std::max<size_t>(1, tspan_pm.size()) * real_size());
+        upload(tspan_dev, tspan_pm.data(), tspan_pm.size());
+    }
+
+    void transient()
+    {
+        require_problem();
+        begin_run();
+        launch(k_transient, 0);
+        end_run("transient");
+        log_msg(CLODE_LOG_INFO, "run transient");
+    }
+
+    // CLODEfeatures::resizeFeaturesVariables (CLODEfeatures.cpp:143-177)
+    void resize_features()
+    {
+        long long nf = (long long)names().size();
+        long long fe = nf * nPts;
+        if (fe != F_elements || obs_words != odata_words_alloc) {
+            F_elements = fe;
+            F.reserve(std::max<long long>(1, fe) * real_size());
+            odata.reserve(std::max<size_t>(1, (size_t)obs_words * nPts) * sizeof(unsigned int));
+            odata_words_alloc = obs_words;
+            observer_initialized = false;
+            log_msg(CLODE_LOG_DEBUG, "resize F, odata with nPts=%lld, nF=%lld", nPts, nf);
+        }
+    }
+
+    void initialize_observer()
+    {
+        require_problem();
+        if (kind != CLODE_SIM_FEATURES)
+            fail(CLODE_ERR_STATE, "not a feature simulator");
+        begin_run();
+        resize_features();
+        launch(k_init, 0);
+        end_run("initializeObserver");
+        observer_initialized = true;
+        log_msg(CLODE_LOG_DEBUG, "run initializeObserver");
+    }
+
+    void features(int reinit)
+    {
+        require_problem();
+        if (kind != CLODE_SIM_FEATURES)
+            fail(CLODE_ERR_STATE, "not a feature simulator");
+        if (reinit >= 0)
+            observer_initialized = reinit == 0;
+        ensure_built();
+        resize_features();
+        int fused = 0;
+        double init_ms = 0.0;
+        if (!observer_initialized) {
+            if (fuse_init) {
+                fused = 1;
+            } else {
+                initialize_observer();
+                init_ms = last_ms;
+            }
+        }
+        begin_run();
+        launch(k_features, fused);
+        end_run("features");
+        last_ms += init_ms;
+        observer_initialized = true;
+        log_msg(CLODE_LOG_DEBUG, "run features");
+    }
+
+    // CLODEtrajectory::resizeTrajectoryVariables (CLODEtrajectory.cpp:45-94)
+    void resize_trajectory()
+    {
+        long long rows = (long long)sp.max_store + 1;  // the kernel may write row max_store
+        if (rows == traj_rows && nPts == traj_pts)
+            return;
+        size_t rs = real_size();
+        double need = (double)rows * nPts * (1 + 2 * nVar + nAux) * rs;
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        if (need > (double)free_b) {
+            long long max_rows = (long long)(free_b / ((double)nPts * (1 + 2 * nVar + nAux) * rs));
+            log_msg(CLODE_LOG_ERR,
+                    "Storage requested exceeds device memory. Try reducing storage to <%lld time points, or reducing nPts.",
+                    max_rows);
+            fail(CLODE_ERR_OUT_OF_MEMORY, "trajectory storage of %.2f GB exceeds free device memory (%.2f GB)",
+                 need / 1e9, free_b / 1e9);
+        }
+        t.reserve(std::max<size_t>(1, rows * nPts) * rs);
+        x.reserve(std::max<size_t>(1, rows * nPts * nVar) * rs);
+        dx.reserve(std::max<size_t>(1, rows * nPts * nVar) * rs);
+        aux.reserve(std::max<size_t>(1, rows * nPts * std::max(nAux, 1)) * rs);
+        nstored.reserve(std::max<size_t>(1, nPts) * sizeof(int));
+        traj_rows = rows;
+        traj_pts = nPts;
+    }
+
+    void trajectory()
+    {
+        require_problem();
+        if (sp.nout == 0)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "solver parameter nout must be at least 1");
+        ensure_built();
+        ensure_stream();
+        resize_trajectory();
+        begin_run();
+        launch(k_trajectory, 0);
+        end_run("trajectory");
+        log_msg(CLODE_LOG_DEBUG, "run trajectory");
+    }
+
+    void shift_x0()
+    {
+        require_problem();
+        ensure_stream();
+        check_cuda(cudaMemcpyAsync(x0.p, xf.p, (size_t)nPts * nVar * real_size(), cudaMemcpyDeviceToDevice, stream),
+                   "shift x0");
+        check_cuda(cudaStreamSynchronize(stream), "shift x0");
+    }
+
+    void shift_tspan()
+    {
+        if (tspan_per_member) {
+            for (size_t i = 0; i + 1 < tspan_pm.size(); i += 2) {
+                double a = tspan_pm[i], b = tspan_pm[i + 1];
+                tspan_pm[i] = b;
+                tspan_pm[i + 1] = b + (b - a);
+            }
+            ensure_stream();
+            sync_tspan_device();
+        } else {
+            double a = tspan[0], b = tspan[1];
+            tspan[0] = b;
+            tspan[1] = b + (b - a);
+        }
+    }
+
+    // --------------------------------------------------------- getters --
+    size_t array_len(int which) const
+    {
+        switch (which) {
+        case CLODE_ARRAY_X0:
+        case CLODE_ARRAY_XF: return (size_t)nPts * nVar;
+        case CLODE_ARRAY_DT:
+        case CLODE_ARRAY_TF: return (size_t)nPts;
+        case CLODE_ARRAY_PARS: return pars_host.size();
+        case CLODE_ARRAY_TSPAN: return tspan_per_member ? tspan_pm.size() : 2;
+        case CLODE_ARRAY_F: return F_elements > 0 ? (size_t)F_elements : 0;
+        case CLODE_ARRAY_T: return traj_rows > 0 ? (size_t)sp.max_store * nPts : 0;
+        case CLODE_ARRAY_X:
+        case CLODE_ARRAY_DX: return traj_rows > 0 ? (size_t)sp.max_store * nPts * nVar : 0;
+        case CLODE_ARRAY_AUX: return traj_rows > 0 ? (nAux > 0 ? (size_t)sp.max_store * nPts * nAux : 1) : 0;
+        }
+        fail(CLODE_ERR_INVALID_ARGUMENT, "unknown array id %d", which);
+    }
+
+    void get(int which, double *out, size_t n)
+    {
+        if (which == CLODE_ARRAY_PARS) {
+            std::copy(pars_host.begin(), pars_host.begin() + n, out);
+            return;
+        }
+        if (which == CLODE_ARRAY_TSPAN) {
+            if (tspan_per_member)
+                std::copy(tspan_pm.begin(), tspan_pm.begin() + n, out);
+            else
+                std::copy(tspan, tspan + n, out);
+            return;
+        }
+        if (n == 0)
+            return;
+        ensure_stream();
+        DevBuf *src = nullptr;
+        switch (which) {
+        case CLODE_ARRAY_X0: src = &x0; break;
+        case CLODE_ARRAY_XF: src = &xf; break;
+        case CLODE_ARRAY_DT: src = &dt; break;
+        case CLODE_ARRAY_TF: src = &tf; break;
+        case CLODE_ARRAY_F: src = &F; break;
+        case CLODE_ARRAY_T: src = &t; break;
+        case CLODE_ARRAY_X: src = &x; break;
+        case CLODE_ARRAY_DX: src = &dx; break;
+        case CLODE_ARRAY_AUX:
+            if (nAux == 0) {
+                out[0] = 0.0;
+                return;
+            }
+            src = &aux;
+            break;
+        }
+        download(*src, out, n);
+    }
+
+    std::string status_report() const
+    {
+        std::ostringstream s;
+        s << "------------------\n   " << rhs_name << "\n   nVar=" << nVar << "\n   nPar=" << nPar
+          << "\n   nAux=" << nAux << "\n   nWiener=" << nWiener << "\nUsing " << (single ? "single" : "double")
+          << " precision.\nUsing stepper: " << stepper << "\n";
+        if (kind == CLODE_SIM_FEATURES)
+            s << "Using observer: " << observer << "\n";
+        return s.str();
+    }
+};
+
+// ==================================================================== C ABI
+namespace {
+
+int set_error(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    log_msg(CLODE_LOG_DEBUG, "error %d: %s", code, msg.c_str());
+    return code;
+}
+
+template <typename F>
+int guard(F &&f)
+{
+    try {
+        f();
+        g_last_error.clear();
+        return CLODE_OK;
+    } catch (const Error &e) {
+        return set_error(e.code, e.what());
+    } catch (const std::bad_alloc &) {
+        return set_error(CLODE_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception &e) {
+        return set_error(CLODE_ERR_INTERNAL, e.what());
+    }
+}
+
+void need(const void *p, const char *what)
+{
+    if (!p)
+        fail(CLODE_ERR_INVALID_ARGUMENT, "%s must not be NULL", what);
+}
+
+void copy_string(const std::string &s, char *buf, size_t cap, size_t *n)
+{
+    if (n)
+        *n = s.size();
+    if (buf && cap) {
+        size_t k = std::min(cap - 1, s.size());
+        memcpy(buf, s.data(), k);
+        buf[k] = 0;
+    }
+}
+
+std::string join(const std::vector<std::string> &v)
+{
+    std::string s;
+    for (size_t i = 0; i < v.size(); ++i) {
+        if (i)
+            s += "\n";
+        s += v[i];
+    }
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *clode_last_error(void) { return g_last_error.c_str(); }
+
+int clode_version(void) { return CLODE_GB300_VERSION; }
+
+int clode_device_count(int *count)
+{
+    return guard([&] {
+        need(count, "count");
+        *count = device_count_or_zero();
+    });
+}
+
+int clode_device_query(int ordinal, clode_device_info *out)
+{
+    return guard([&] {
+        need(out, "out");
+        int n = device_count_or_zero();
+        if (ordinal < 0 || ordinal >= n)
+            fail(CLODE_ERR_NO_DEVICE, "CUDA device %d does not exist (%d present)", ordinal, n);
+        cudaDeviceProp p;
+        check_cuda(cudaGetDeviceProperties(&p, ordinal), "cudaGetDeviceProperties");
+        memset(out, 0, sizeof *out);
+        snprintf(out->name, sizeof out->name, "%s", p.name);
+        snprintf(out->vendor, sizeof out->vendor, "NVIDIA Corporation");
+        int rt = 0, drv = 0;
+        cudaRuntimeGetVersion(&rt);
+        cudaDriverGetVersion(&drv);
+        snprintf(out->version, sizeof out->version, "CUDA %d.%d (driver %d.%d)", rt / 1000, (rt % 1000) / 10,
+                 drv / 1000, (drv % 1000) / 10);
+        out->ordinal = ordinal;
+        out->compute_units = p.multiProcessorCount;
+        out->cc_major = p.major;
+        out->cc_minor = p.minor;
+        int khz = 0;
+        cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, ordinal);
+        out->max_clock_mhz = khz / 1000;
+        out->max_work_group_size = p.maxThreadsPerBlock;
+        out->double_support = 1;
+        out->device_memory_size = p.totalGlobalMem;
+        out->max_memory_alloc_size = p.totalGlobalMem;
+    });
+}
+
+int clode_set_cache_dir(const char *dir)
+{
+    return guard([&] { set_cache_dir(dir ? dir : ""); });
+}
+
+int clode_sim_create(int kind, const clode_problem *prob, const char *stepper, const char *observer,
+                     const clode_observer_params *op, int single_precision, int device, clode_sim **out)
+{
+    return guard([&] {
+        need(out, "out");
+        *out = nullptr;
+        if (kind < CLODE_SIM_BASE || kind > CLODE_SIM_TRAJECTORY)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "unknown simulator kind %d", kind);
+        std::unique_ptr<clode_sim> s(new clode_sim());
+        s->kind = kind;
+        s->set_problem(prob);
+        s->set_stepper(stepper);
+        if (s->stepper.empty())
+            fail(CLODE_ERR_INVALID_ARGUMENT, "Unknown stepper: %s", stepper ? stepper : "(null)");
+        s->single = single_precision != 0;
+        s->device = device;
+        if (kind == CLODE_SIM_FEATURES) {
+            if (op)
+                s->op = *op;
+            s->set_observer(observer);
+            if (s->observer.empty())
+                fail(CLODE_ERR_INVALID_ARGUMENT, "unknown observer: %s", observer ? observer : "(null)");
+        }
+        *out = s.release();
+    });
+}
+
+int clode_sim_destroy(clode_sim *sim)
+{
+    return guard([&] { delete sim; });
+}
+
+#define SIM_GUARD(body)                 \
+    return guard([&] {                  \
+        need(sim, "sim");               \
+        body;                           \
+    })
+
+int clode_sim_set_problem_info(clode_sim *sim, const clode_problem *prob) { SIM_GUARD(sim->set_problem(prob)); }
+int clode_sim_set_stepper(clode_sim *sim, const char *stepper) { SIM_GUARD(sim->set_stepper(stepper)); }
+int clode_sim_set_precision(clode_sim *sim, int single_precision)
+{
+    SIM_GUARD({
+        if ((single_precision != 0) != sim->single) {
+            sim->single = single_precision != 0;
+            sim->built = false;
+            sim->nPts = -1;  // device buffers are re-made at the next set_problem_data
+        }
+    });
+}
+int clode_sim_set_device(clode_sim *sim, int device)
+{
+    SIM_GUARD({
+        if (device != sim->device) {
+            sim->device = device;
+            sim->built = false;
+            sim->nPts = -1;
+        }
+    });
+}
+int clode_sim_set_observer(clode_sim *sim, const char *observer)
+{
+    SIM_GUARD({
+        if (sim->kind != CLODE_SIM_FEATURES)
+            fail(CLODE_ERR_STATE, "not a feature simulator");
+        sim->set_observer(observer);
+    });
+}
+int clode_sim_build(clode_sim *sim) { SIM_GUARD(sim->build()); }
+
+int clode_sim_set_problem_data(clode_sim *sim, const double *x0, size_t n_x0, const double *pars, size_t n_pars)
+{
+    SIM_GUARD({
+        if (n_x0)
+            need(x0, "x0");
+        if (n_pars)
+            need(pars, "pars");
+        sim->set_problem_data(x0, n_x0, pars, n_pars);
+    });
+}
+int clode_sim_set_x0(clode_sim *sim, const double *x0, size_t n)
+{
+    SIM_GUARD({
+        if (n)
+            need(x0, "x0");
+        sim->set_x0(x0, n);
+    });
+}
+int clode_sim_set_pars(clode_sim *sim, const double *pars, size_t n)
+{
+    SIM_GUARD({
+        if (n)
+            need(pars, "pars");
+        sim->set_pars(pars, n);
+    });
+}
+int clode_sim_set_tspan(clode_sim *sim, const double *tspan2)
+{
+    SIM_GUARD({
+        need(tspan2, "tspan");
+        sim->tspan[0] = tspan2[0];
+        sim->tspan[1] = tspan2[1];
+        sim->tspan_per_member = false;
+    });
+}
+int clode_sim_set_tspan_per_member(clode_sim *sim, const double *tspan, size_t n)
+{
+    SIM_GUARD({
+        if ((long long)n != 2 * sim->nPts || sim->nPts <= 0)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "per-member tspan needs 2*nPts=%lld values, received %zu",
+                 2 * sim->nPts, n);
+        need(tspan, "tspan");
+        sim->tspan_pm.assign(tspan, tspan + n);
+        sim->tspan_per_member = true;
+        sim->ensure_stream();
+        sim->sync_tspan_device();
+    });
+}
+int clode_sim_set_solver_params(clode_sim *sim, const clode_solver_params *sp)
+{
+    SIM_GUARD({
+        need(sp, "solver params");
+        sim->sp = *sp;  // device dt is reset only when nPts changes (CLODE.cpp:377-402)
+    });
+}
+int clode_sim_get_solver_params(clode_sim *sim, clode_solver_params *sp)
+{
+    SIM_GUARD({
+        need(sp, "solver params");
+        *sp = sim->sp;
+    });
+}
+int clode_sim_set_observer_params(clode_sim *sim, const clode_observer_params *op)
+{
+    SIM_GUARD({
+        need(op, "observer params");
+        sim->op = *op;
+    });
+}
+int clode_sim_get_observer_params(clode_sim *sim, clode_observer_params *op)
+{
+    SIM_GUARD({
+        need(op, "observer params");
+        *op = sim->op;
+    });
+}
+int clode_sim_seed_rng(clode_sim *sim, int use_seed, int seed) { SIM_GUARD(sim->seed_rng(use_seed != 0, seed)); }
+int clode_sim_transient(clode_sim *sim) { SIM_GUARD(sim->transient()); }
+int clode_sim_initialize_observer(clode_sim *sim) { SIM_GUARD(sim->initialize_observer()); }
+int clode_sim_features(clode_sim *sim, int reinitialize) { SIM_GUARD(sim->features(reinitialize)); }
+int clode_sim_is_observer_initialized(clode_sim *sim, int *initialized)
+{
+    SIM_GUARD({
+        need(initialized, "initialized");
+        *initialized = sim->observer_initialized ? 1 : 0;
+    });
+}
+int clode_sim_trajectory(clode_sim *sim) { SIM_GUARD(sim->trajectory()); }
+int clode_sim_shift_tspan(clode_sim *sim) { SIM_GUARD(sim->shift_tspan()); }
+int clode_sim_shift_x0(clode_sim *sim) { SIM_GUARD(sim->shift_x0()); }
+
+int clode_sim_get_sizes(clode_sim *sim, clode_sizes *out)
+{
+    SIM_GUARD({
+        need(out, "out");
+        out->n_pts = std::max<long long>(0, sim->nPts);
+        out->n_var = sim->nVar;
+        out->n_par = sim->nPar;
+        out->n_aux = sim->nAux;
+        out->n_wiener = sim->nWiener;
+        out->n_features = sim->kind == CLODE_SIM_FEATURES ? (long long)sim->names().size() : 0;
+        out->max_store = sim->sp.max_store;
+        out->t_elements = (long long)sim->array_len(CLODE_ARRAY_T);
+        out->x_elements = (long long)sim->array_len(CLODE_ARRAY_X);
+        out->aux_elements = (long long)sim->array_len(CLODE_ARRAY_AUX);
+    });
+}
+
+int clode_sim_get(clode_sim *sim, int which, double *out, size_t capacity, size_t *n)
+{
+    SIM_GUARD({
+        size_t len = sim->nPts < 0 ? 0 : sim->array_len(which);
+        if (n)
+            *n = len;
+        if (!out)
+            return;
+        if (capacity < len)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "output capacity %zu is smaller than the array (%zu)", capacity, len);
+        sim->get(which, out, len);
+    });
+}
+
+int clode_sim_get_n_stored(clode_sim *sim, int *out, size_t capacity, size_t *n)
+{
+    SIM_GUARD({
+        size_t len = sim->traj_rows > 0 ? (size_t)sim->nPts : 0;
+        if (n)
+            *n = len;
+        if (!out || !len)
+            return;
+        if (capacity < len)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "output capacity %zu is smaller than nPts (%zu)", capacity, len);
+        sim->ensure_stream();
+        check_cuda(cudaMemcpy(out, sim->nstored.p, len * sizeof(int), cudaMemcpyDeviceToHost), "D2H copy");
+    });
+}
+
+int clode_sim_get_status(clode_sim *sim, int *out, size_t capacity, size_t *n)
+{
+    SIM_GUARD({
+        size_t len = sim->nPts > 0 ? (size_t)sim->nPts : 0;
+        if (n)
+            *n = len;
+        if (!out || !len)
+            return;
+        if (capacity < len)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "output capacity %zu is smaller than nPts (%zu)", capacity, len);
+        sim->ensure_stream();
+        check_cuda(cudaMemcpy(out, sim->status.p, len * sizeof(int), cudaMemcpyDeviceToHost), "D2H copy");
+    });
+}
+
+int clode_sim_get_stats(clode_sim *sim, unsigned long long *out)
+{
+    SIM_GUARD({
+        need(out, "out");
+        memcpy(out, sim->last_stats, sizeof sim->last_stats);
+    });
+}
+
+int clode_sim_last_kernel_ms(clode_sim *sim, double *ms)
+{
+    SIM_GUARD({
+        need(ms, "ms");
+        *ms = sim->last_ms;
+    });
+}
+
+int clode_sim_get_string(clode_sim *sim, int which, char *buf, size_t capacity, size_t *n)
+{
+    SIM_GUARD({
+        std::string s;
+        switch (which) {
+        case CLODE_STRING_PROGRAM:
+            s = sim->built ? "// options: " + sim->prog.options + "\n" + sim->prog.source : std::string();
+            break;
+        case CLODE_STRING_FEATURE_NAMES: s = join(sim->names()); break;
+        case CLODE_STRING_AVAILABLE_STEPPERS: {
+            std::vector<std::string> v;
+            for (auto &kv : kSteppers)
+                v.push_back(kv.first);
+            s = join(v);
+            break;
+        }
+        case CLODE_STRING_AVAILABLE_OBSERVERS: {
+            std::vector<std::string> v;
+            for (auto &kv : kObservers)
+                v.push_back(kv.first);
+            s = join(v);
+            break;
+        }
+        case CLODE_STRING_OBSERVER_NAME: s = sim->observer; break;
+        case CLODE_STRING_STEPPER: s = sim->stepper; break;
+        case CLODE_STRING_STATUS_REPORT: s = sim->status_report(); break;
+        case CLODE_STRING_BUILD_LOG: s = sim->prog.log; break;
+        default: fail(CLODE_ERR_INVALID_ARGUMENT, "unknown string id %d", which);
+        }
+        copy_string(s, buf, capacity, n);
+    });
+}
+
+int clode_sim_set_option(clode_sim *sim, const char *key, double value)
+{
+    SIM_GUARD({
+        need(key, "key");
+        std::string k = key;
+        if (k == "schedule") {
+            sim->schedule = (int)value;
+        } else if (k == "block_size") {
+            if (value < 32 || value > 1024)
+                fail(CLODE_ERR_INVALID_ARGUMENT, "block_size must be in [32, 1024]");
+            sim->block_size = (int)value;
+        } else if (k == "blocks_per_sm") {
+            sim->blocks_per_sm = (int)value;
+        } else if (k == "fmad") {
+            bool v = value != 0.0;
+            if (v != sim->fmad) {
+                sim->fmad = v;
+                sim->built = false;
+            }
+        } else if (k == "time_budget_ms") {
+            sim->time_budget_ms = value;
+        } else if (k == "fuse_init") {
+            sim->fuse_init = value != 0.0;
+        } else if (k == "collect_stats") {
+            sim->collect_stats = value != 0.0;
+        } else {
+            fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);
+        }
+    });
+}
+
+int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
+{
+    SIM_GUARD({
+        need(key, "key");
+        need(value, "value");
+        std::string k = key;
+        if (k == "schedule") *value = sim->schedule;
+        else if (k == "block_size") *value = sim->block_size;
+        else if (k == "blocks_per_sm") *value = sim->blocks_per_sm;
+        else if (k == "fmad") *value = sim->fmad;
+        else if (k == "time_budget_ms") *value = sim->time_budget_ms;
+        else if (k == "fuse_init") *value = sim->fuse_init;
+        else if (k == "collect_stats") *value = sim->collect_stats;
+        else fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);
+    });
+}
+
+int clode_sim_kernel_info(clode_sim *sim, const char *kernel, int *registers, int *max_threads)
+{
+    SIM_GUARD({
+        need(kernel, "kernel");
+        sim->ensure_built();
+        std::string k = kernel;
+        cudaKernel_t kk = k == "transient" ? sim->k_transient
+                          : k == "trajectory" ? sim->k_trajectory
+                          : k == "init_observer" ? sim->k_init
+                          : k == "features" ? sim->k_features : nullptr;
+        if (!kk)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "no kernel '%s' in this program", kernel);
+        cudaFuncAttributes fa;
+        check_cuda(cudaFuncGetAttributes(&fa, (const void *)kk), "cudaFuncGetAttributes");
+        if (registers)
+            *registers = fa.numRegs;
+        if (max_threads)
+            *max_threads = fa.maxThreadsPerBlock;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,247 @@
+/*
+ * clode_gb300 — C ABI of the GB300 ensemble ODE/SDE engine.
+ *
+ * This is the boundary a host language binds (ctypes, cgo, JNI, N-API ...).
+ * It replaces the OpenCL resource/program layer and the three simulator
+ * classes of clODE (clode/cpp/OpenCLResource.hpp:73-125, clode/cpp/CLODE.hpp:93-189,
+ * clode/cpp/CLODEfeatures.hpp:23-76, clode/cpp/CLODEtrajectory.hpp:21-52) that
+ * clODE's pybind11 module clode_cpp_wrapper exposes (clode/cpp/CLODEpython.cpp:35-381).
+ * Each entry point below names the reference member function it stands in for.
+ *
+ * Conventions
+ *  - Every function returns CLODE_OK (0) or a CLODE_ERR_* code; the message of
+ *    the last error on the calling thread is returned by clode_last_error().
+ *  - Host arrays are double, SoA column-major exactly as clODE's host side
+ *    takes them: x0[j*nPts + i], pars[j*nPts + i] (clode/cpp/CLODE.cpp:245-350),
+ *    features F[k*nPts + i], trajectories [store*nPts*n + j*nPts + i].
+ *    Single-precision simulators convert on the device.
+ *  - Calls on one simulator are synchronous (every run ends with a stream
+ *    synchronize, as the reference ends every launch with finish()) and not
+ *    thread-safe; different simulators may be driven from different threads.
+ *  - Size mismatches in set_x0 / set_pars / set_problem_data are reported as
+ *    CLODE_ERR_INVALID_ARGUMENT (the reference logs and ignores them,
+ *    clode/cpp/CLODE.cpp:247-271,309-349); nothing is changed in that case.
+ *  - No entry point falls back to the CPU: without a usable CUDA device, run
+ *    calls fail with CLODE_ERR_NO_DEVICE.
+ */
+#ifndef CLODE_GB300_H
+#define CLODE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CLODE_GB300_VERSION 100
+
+enum clode_status {
+    CLODE_OK = 0,
+    CLODE_ERR_INVALID_ARGUMENT = 1,
+    CLODE_ERR_CUDA = 2,
+    CLODE_ERR_COMPILE = 3,
+    CLODE_ERR_NOT_BUILT = 4,
+    CLODE_ERR_NO_DEVICE = 5,
+    CLODE_ERR_OUT_OF_MEMORY = 6,
+    CLODE_ERR_STATE = 7,
+    CLODE_ERR_INTERNAL = 8
+};
+
+/* simulator kinds: CLODE, CLODEfeatures, CLODEtrajectory */
+enum clode_sim_kind { CLODE_SIM_BASE = 0, CLODE_SIM_FEATURES = 1, CLODE_SIM_TRAJECTORY = 2 };
+
+/* arrays readable with clode_sim_get() */
+enum clode_array {
+    CLODE_ARRAY_X0 = 0,     /* CLODE::getX0       clode/cpp/CLODE.cpp:517   */
+    CLODE_ARRAY_XF = 1,     /* CLODE::getXf       clode/cpp/CLODE.cpp:534   */
+    CLODE_ARRAY_DT = 2,     /* CLODE::getDt       clode/cpp/CLODE.cpp:551   */
+    CLODE_ARRAY_TF = 3,     /* CLODE::getTf       clode/cpp/CLODE.cpp:568   */
+    CLODE_ARRAY_PARS = 4,   /* CLODE::getPars     clode/cpp/CLODE.hpp:180   */
+    CLODE_ARRAY_TSPAN = 5,  /* CLODE::getTspan    clode/cpp/CLODE.hpp:178 (2 values, or 2*nPts per member) */
+    CLODE_ARRAY_F = 6,      /* CLODEfeatures::getF         clode/cpp/CLODEfeatures.cpp:261 */
+    CLODE_ARRAY_T = 7,      /* CLODEtrajectory::getT       clode/cpp/CLODEtrajectory.cpp:132 */
+    CLODE_ARRAY_X = 8,      /* CLODEtrajectory::getX       clode/cpp/CLODEtrajectory.cpp:149 */
+    CLODE_ARRAY_DX = 9,     /* CLODEtrajectory::getDx      clode/cpp/CLODEtrajectory.cpp:166 */
+    CLODE_ARRAY_AUX = 10    /* CLODEtrajectory::getAux     clode/cpp/CLODEtrajectory.cpp:183 */
+};
+
+/* strings readable with clode_sim_get_string() */
+enum clode_string {
+    CLODE_STRING_PROGRAM = 0,             /* CLODE::getProgramString          CLODE.hpp:187 */
+    CLODE_STRING_FEATURE_NAMES = 1,       /* CLODEfeatures::getFeatureNames   CLODEfeatures.hpp:74, '\n'-separated */
+    CLODE_STRING_AVAILABLE_STEPPERS = 2,  /* CLODE::getAvailableSteppers      CLODE.hpp:185 */
+    CLODE_STRING_AVAILABLE_OBSERVERS = 3, /* CLODEfeatures::getAvailableObservers CLODEfeatures.hpp:75 */
+    CLODE_STRING_OBSERVER_NAME = 4,       /* CLODEfeatures::getObserverName   CLODEfeatures.hpp:71 */
+    CLODE_STRING_STEPPER = 5,
+    CLODE_STRING_STATUS_REPORT = 6,       /* CLODE::printStatus text          CLODE.cpp:585-596 */
+    CLODE_STRING_BUILD_LOG = 7
+};
+
+/* launch-wide counters, clode_sim_get_stats() */
+enum clode_stat {
+    CLODE_STAT_STEPS = 0,      /* time-loop iterations (accepted steps and hmin failures) */
+    CLODE_STAT_REJECTED = 1,   /* rejected adaptive attempts */
+    CLODE_STAT_RHS_EVALS = 2,  /* right-hand-side evaluations, all passes */
+    CLODE_STAT_EVENTS = 3,     /* observer events */
+    CLODE_STAT_COUNT = 8
+};
+
+/* per-member status bits, clode_sim_get_status() */
+enum clode_member_status {
+    CLODE_MEMBER_HMIN_FAIL = 1,
+    CLODE_MEMBER_NONFINITE = 2,
+    CLODE_MEMBER_MAX_STEPS = 4,
+    CLODE_MEMBER_TERMINAL_EVENT = 8,
+    CLODE_MEMBER_TIME_BUDGET = 16
+};
+
+/* log levels: the values of spdlog::level used by clODE's LogLevel enum
+ * (clode/cpp/CLODEpython.cpp:43-51) */
+enum clode_log_level {
+    CLODE_LOG_TRACE = 0, CLODE_LOG_DEBUG = 1, CLODE_LOG_INFO = 2, CLODE_LOG_WARN = 3,
+    CLODE_LOG_ERR = 4, CLODE_LOG_CRITICAL = 5, CLODE_LOG_OFF = 6
+};
+
+/* ProblemInfo, clode/cpp/CLODE.hpp:22-91.  rhs_source is the model's getRHS
+ * source text (the reference reads it from ProblemInfo::clRHSfilename). */
+typedef struct clode_problem {
+    const char *rhs_source;
+    const char *rhs_name;       /* used in diagnostics only; may be NULL */
+    int n_var, n_par, n_aux, n_wiener;
+    const char *var_names;      /* '\n'-separated, n_var entries (feature names) */
+    const char *par_names;      /* '\n'-separated, may be NULL */
+    const char *aux_names;      /* '\n'-separated, n_aux entries */
+} clode_problem;
+
+/* SolverParams<double>, clode/cpp/clODE_struct_defs.cl:11-20 */
+typedef struct clode_solver_params {
+    double dt, dtmax, abstol, reltol;
+    unsigned int max_steps, max_store, nout;
+} clode_solver_params;
+
+/* ObserverParams<double>, clode/cpp/observers.cl:25-46 */
+typedef struct clode_observer_params {
+    unsigned int e_var_ix, f_var_ix, max_event_count, max_event_timestamps;
+    double min_x_amp, min_imi, nhood_radius, x_up_thresh, x_down_thresh;
+    double dx_up_thresh, dx_down_thresh, eps_dx;
+} clode_observer_params;
+
+/* DeviceInfo, clode/cpp/OpenCLResource.hpp:33-50 */
+typedef struct clode_device_info {
+    char name[256];
+    char vendor[64];
+    char version[64];
+    int ordinal;
+    int compute_units;            /* SM count */
+    int cc_major, cc_minor;
+    int max_clock_mhz;
+    int max_work_group_size;      /* max threads per block */
+    int double_support;
+    unsigned long long device_memory_size;
+    unsigned long long max_memory_alloc_size;
+} clode_device_info;
+
+typedef struct clode_sim clode_sim;
+
+/* ---------------------------------------------------------------- runtime */
+/* Message of the last failed call on this thread ("" if none). */
+const char *clode_last_error(void);
+int clode_version(void);
+/* Number of CUDA devices (OpenCLResource::getPlatformAndDevices, OpenCLResource.cpp:130-200). */
+int clode_device_count(int *count);
+/* DeviceInfo of one device (OpenCLResource::getDeviceInfo / query_opencl, CLODEpython.cpp:134-176). */
+int clode_device_query(int ordinal, clode_device_info *out);
+
+/* LoggerSingleton (clode/cpp/CLODEpython.cpp:53-95): level, pattern and an
+ * optional sink that receives every formatted message instead of stdout. */
+typedef void (*clode_log_sink_fn)(int level, const char *message);
+int clode_log_set_level(int level);
+int clode_log_get_level(void);
+int clode_log_set_pattern(const char *pattern);
+int clode_log_set_sink(clode_log_sink_fn sink);
+int clode_log_message(int level, const char *message);
+
+/* Directory of the on-disk cache of compiled ensemble programs (NULL: default). */
+int clode_set_cache_dir(const char *dir);
+
+/* -------------------------------------------------------------- simulator */
+/* CLODE / CLODEfeatures / CLODEtrajectory constructors
+ * (CLODE.cpp:13-24, CLODEfeatures.cpp:9-18, CLODEtrajectory.cpp:9-14).
+ * observer/op are used by CLODE_SIM_FEATURES only (may be NULL otherwise).
+ * device is a CUDA ordinal. */
+int clode_sim_create(int kind, const clode_problem *prob, const char *stepper, const char *observer,
+                     const clode_observer_params *op, int single_precision, int device, clode_sim **out);
+int clode_sim_destroy(clode_sim *sim);
+
+/* setters that require clode_sim_build() afterwards */
+int clode_sim_set_problem_info(clode_sim *sim, const clode_problem *prob); /* CLODE::setProblemInfo  CLODE.cpp:43 */
+int clode_sim_set_stepper(clode_sim *sim, const char *stepper);           /* CLODE::setStepper      CLODE.cpp:61 */
+int clode_sim_set_precision(clode_sim *sim, int single_precision);        /* CLODE::setPrecision    CLODE.cpp:78 */
+int clode_sim_set_device(clode_sim *sim, int device);                     /* CLODE::setOpenCL       CLODE.cpp:88 */
+int clode_sim_set_observer(clode_sim *sim, const char *observer);         /* CLODEfeatures::setObserver CLODEfeatures.cpp:63 */
+/* compile the ensemble program with NVRTC (cached on disk) */
+int clode_sim_build(clode_sim *sim);                                      /* CLODE::buildCL         CLODE.cpp:155 */
+
+/* problem data (CLODE.cpp:245-402) */
+int clode_sim_set_problem_data(clode_sim *sim, const double *x0, size_t n_x0, const double *pars, size_t n_pars);
+int clode_sim_set_x0(clode_sim *sim, const double *x0, size_t n);
+int clode_sim_set_pars(clode_sim *sim, const double *pars, size_t n);
+int clode_sim_set_tspan(clode_sim *sim, const double *tspan2);
+int clode_sim_set_solver_params(clode_sim *sim, const clode_solver_params *sp);
+int clode_sim_get_solver_params(clode_sim *sim, clode_solver_params *sp);
+int clode_sim_set_observer_params(clode_sim *sim, const clode_observer_params *op); /* CLODEfeatures.cpp:78 */
+int clode_sim_get_observer_params(clode_sim *sim, clode_observer_params *op);
+/* CLODE::seedRNG() / seedRNG(int) (CLODE.cpp:420-465): use_seed = 0 draws a random seed */
+int clode_sim_seed_rng(clode_sim *sim, int use_seed, int seed);
+
+/* runs (CLODE.cpp:468-515, CLODEfeatures.cpp:180-259, CLODEtrajectory.cpp:97-130) */
+int clode_sim_transient(clode_sim *sim);
+int clode_sim_initialize_observer(clode_sim *sim);
+/* reinitialize: -1 = features(), 0/1 = features(bool reinitialize_observer) */
+int clode_sim_features(clode_sim *sim, int reinitialize);
+int clode_sim_is_observer_initialized(clode_sim *sim, int *initialized);
+int clode_sim_trajectory(clode_sim *sim);
+int clode_sim_shift_tspan(clode_sim *sim);
+int clode_sim_shift_x0(clode_sim *sim);
+
+/* sizes: nPts, nFeatures, and element counts of every readable array */
+typedef struct clode_sizes {
+    long long n_pts, n_var, n_par, n_aux, n_wiener, n_features;
+    long long max_store;         /* rows of the trajectory arrays */
+    long long t_elements, x_elements, aux_elements;
+} clode_sizes;
+int clode_sim_get_sizes(clode_sim *sim, clode_sizes *out);
+/* copy an array to host doubles; *n receives its length. With out == NULL only *n is set. */
+int clode_sim_get(clode_sim *sim, int which, double *out, size_t capacity, size_t *n);
+int clode_sim_get_n_stored(clode_sim *sim, int *out, size_t capacity, size_t *n); /* CLODEtrajectory::getNstored */
+int clode_sim_get_string(clode_sim *sim, int which, char *buf, size_t capacity, size_t *n);
+
+/* ------------------------------------------- additions (no reference counterpart) */
+/* Per-member time spans: tspan[2*i], tspan[2*i+1] for member i (n = 2*nPts).
+ * Replaces the single global tspan until clode_sim_set_tspan() is called again. */
+int clode_sim_set_tspan_per_member(clode_sim *sim, const double *tspan, size_t n);
+/* Per-member status bits of the last run (CLODE_MEMBER_*). */
+int clode_sim_get_status(clode_sim *sim, int *out, size_t capacity, size_t *n);
+/* Launch-wide counters of the last run (CLODE_STAT_*; out has CLODE_STAT_COUNT slots). */
+int clode_sim_get_stats(clode_sim *sim, unsigned long long *out);
+/* Device time of the last run's kernel launches in milliseconds (CUDA events on the simulator's stream). */
+int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
+/* Engine options: "schedule" (0 grid, 1 persistent), "block_size", "blocks_per_sm",
+ * "fmad" (0/1: allow contraction of a*b+c; 0 reproduces the reference bit for bit),
+ * "time_budget_ms" (persistent launches stop taking new members after it),
+ * "fuse_init" (0/1: run the observer initialisation inside the features launch),
+ * "collect_stats" (0/1). */
+int clode_sim_set_option(clode_sim *sim, const char *key, double value);
+int clode_sim_get_option(clode_sim *sim, const char *key, double *value);
+/* Number of kernel launches this library has issued since it was loaded
+ * (ensemble kernels and the conversion/seeding kernels alike). */
+unsigned long long clode_launch_count(void);
+/* Register-file footprint of the built kernels: registers per thread of the features
+ * (or transient / trajectory) kernel, as reported by the driver. */
+int clode_sim_kernel_info(clode_sim *sim, const char *kernel, int *registers, int *max_threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CLODE_GB300_H */

@@ -1,0 +1,176 @@
+"""Parity of the CUDA engine (called through the drop-in API and the C ABI)
+with the CPU oracle on identical seeded inputs.
+
+Tolerances:
+  * fixed-step steppers (Euler, Heun, RK4) on models built from + - * /
+    only: bitwise equality of final states, times, step sizes and every
+    feature, in FP64 and FP32 (the engine reproduces the reference's
+    operation order with contraction off);
+  * anything that calls a transcendental function — the adaptive
+    controller's pow, exp in the lactotroph model, log in the normal
+    deviates — differs from the CPU's libm in the last bit now and then, so
+    those runs are compared with a relative tolerance written in each test,
+    event counts exactly for all but a stated fraction of members.
+"""
+import numpy as np
+import pytest
+
+from tests.parity import Scenario, assert_bitwise, mismatch_fraction, run_engine, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+SEED = 20261203
+
+
+def vdp_inputs(n, seed=SEED):
+    rng = np.random.default_rng(seed)
+    mu = rng.uniform(0.1, 5.0, n)
+    x0 = rng.uniform(-2.0, 2.0, (n, 2))
+    return x0, mu[:, None]
+
+
+def lorenz_inputs(n, seed=SEED):
+    rng = np.random.default_rng(seed)
+    x0 = np.ones((n, 3)) + rng.normal(0.0, 1e-3, (n, 3))
+    rho = rng.uniform(10, 60, n)
+    sigma = rng.uniform(5, 15, n)
+    return x0, np.stack([rho, sigma, np.full(n, 8.0 / 3.0)], axis=1)
+
+
+def test_vdp_rk4_fp64_localmax_bitwise():
+    x0, p = vdp_inputs(512)
+    sc = Scenario("van_der_pol.cl", 2, 1, x0, p, stepper="rk4", observer="localmax", single=False,
+                  sp=dict(dt=0.01, max_steps=10000000),
+                  steps=[("transient", (0.0, 20.0)), ("shift_x0",), ("features", (20.0, 100.0))])
+    eng, ora = run_engine(sc), run_oracle(sc)
+    assert_bitwise(eng, ora)
+    F = eng["F_list"][0]
+    names = eng["feature_names"]
+    assert len(names) == F.shape[1] == 18
+    # every member oscillates: several local maxima, positive mean period
+    assert (F[:, names.index("event count")] >= 3).all()
+    assert (F[:, names.index("mean IMI")] > 0).all()
+
+
+@pytest.mark.parametrize("stepper", ["euler", "heun", "rk4"])
+@pytest.mark.parametrize("observer", ["basic", "basicall", "localmax", "nhood1", "nhood2", "thresh2"])
+@pytest.mark.parametrize("single", [False, True])
+def test_fixed_steppers_all_observers_bitwise(stepper, observer, single):
+    x0, p = lorenz_inputs(256)
+    sc = Scenario("lorenz.cl", 3, 3, x0, p, n_aux=1, stepper=stepper, observer=observer, single=single,
+                  n_store_events=3 if observer in ("thresh2", "nhood2") else 0,
+                  sp=dict(dt=0.005, max_steps=100000),
+                  op=dict(e_var_ix=2, f_var_ix=2, max_event_count=10000, x_up_threshold=0.3,
+                          x_down_threshold=0.2, nhood_radius=0.1),
+                  steps=[("features", (0.0, 10.0)), ("shift_x0",), ("shift_tspan",), ("features", None)])
+    eng, ora = run_engine(sc), run_oracle(sc)
+    assert_bitwise(eng, ora)
+
+
+@pytest.mark.parametrize("single", [False, True])
+def test_fixed_steppers_trajectory_bitwise(single):
+    x0, p = vdp_inputs(300)
+    sc = Scenario("van_der_pol.cl", 2, 1, x0, p, stepper="rk4", single=single,
+                  sp=dict(dt=0.01, max_store=500, nout=3),
+                  steps=[("trajectory", (0.0, 20.0))])
+    eng, ora = run_engine(sc), run_oracle(sc)
+    assert_bitwise(eng, ora, keys=("xf", "tf", "dt", "t", "x", "dx", "n_stored"))
+    # max_store bounds the rows: 500 stored rows stop the run at step 1500 (t = 15), before t = 20
+    assert (eng["n_stored"] == 500).all()
+    assert np.allclose(eng["tf"], 15.0, atol=1e-4)
+
+
+@pytest.mark.parametrize("stepper", ["bs23", "dopri5"])
+@pytest.mark.parametrize("single", [False, True])
+def test_adaptive_thresh2_close(stepper, single):
+    x0, p = vdp_inputs(256)
+    sc = Scenario("van_der_pol.cl", 2, 1, x0, p, stepper=stepper, observer="thresh2", single=single,
+                  sp=dict(dt=0.01, dtmax=0.5, abstol=1e-9 if not single else 1e-6, reltol=1e-6 if not single else 1e-4,
+                          max_steps=1000000),
+                  op=dict(e_var_ix=0, f_var_ix=0, max_event_count=10000, x_up_threshold=0.3, x_down_threshold=0.2),
+                  steps=[("features", (0.0, 200.0))])
+    eng, ora = run_engine(sc), run_oracle(sc)
+    F, G = eng["F_list"][0], ora["F_list"][0]
+    names = eng["feature_names"]
+    # tolerance: pow() in the step-size controller may differ by an ulp between
+    # CUDA and the host libm; solutions then agree to the integration tolerance
+    rtol = 1e-6 if not single else 2e-3
+    ev = names.index("event count")
+    assert (np.abs(F[:, ev] - G[:, ev]) <= 1).all()
+    assert np.mean(F[:, ev] == G[:, ev]) >= 0.98
+    per = names.index("mean period")
+    assert mismatch_fraction(F[:, per], G[:, per], rtol=rtol * 10, atol=1e-6) <= 0.02
+    assert mismatch_fraction(eng["xf"], ora["xf"], rtol=1e-3 if single else 1e-5, atol=1e-5) <= 0.05
+
+
+def test_lactotroph_transient_published_state():
+    # samples/test_outputs_cpp.md:10 of the reference: RK4 dt=0.1 over [0,1000],
+    # FP32, x0 = 0, (gcal, gsk, gbk) = (1.5, 3, 1): -64.7058 0.022137 6.25581e-06 0.209086
+    n = 32
+    sc = Scenario("lactotroph.cl", 4, 3, np.zeros((n, 4)), np.tile([1.5, 3.0, 1.0], (n, 1)), n_aux=1,
+                  stepper="rk4", single=True,
+                  sp=dict(dt=0.1, dtmax=1.0, max_steps=10000000, nout=50),
+                  steps=[("transient", (0.0, 1000.0)), ("transient", (0.0, 1000.0))])
+    eng = run_engine(sc)
+    xf = eng["xf"][0]
+    np.testing.assert_allclose(xf, [-64.7058, 0.022137, 6.25581e-06, 0.209086], rtol=2e-5)
+    ora = run_oracle(sc)
+    # tolerance: expf differs between CUDA and the host libm in the last bit
+    np.testing.assert_allclose(eng["xf"], ora["xf"], rtol=1e-4, atol=1e-9)
+
+
+def test_ou_trajectory_seuler_fp32():
+    # 16 parameter points x 16 realisations, Euler-Maruyama dt=1e-3, every 10th step stored
+    th = np.linspace(0.1, 2.0, 4)
+    sg = np.linspace(0.1, 1.0, 4)
+    TH, SG = np.meshgrid(th, sg, indexing="ij")
+    reps = 16
+    pars = np.stack([np.repeat(TH.ravel(), reps), np.zeros(16 * reps), np.repeat(SG.ravel(), reps)], axis=1)
+    n = pars.shape[0]
+    sc = Scenario("ornstein_uhlenbeck.cl", 1, 3, np.zeros((n, 1)), pars, n_wiener=1, stepper="seuler", single=True,
+                  sp=dict(dt=1e-3, max_steps=5000, max_store=502, nout=10), seed=7,
+                  steps=[("trajectory", (0.0, 5.0))])
+    eng, ora = run_engine(sc), run_oracle(sc)
+    assert (eng["n_stored"] == ora["n_stored"]).all()
+    assert (eng["n_stored"] == 500).all()
+    np.testing.assert_array_equal(eng["t"], ora["t"])
+    # tolerance: logf in the normal deviates may differ by an ulp from the host libm
+    np.testing.assert_allclose(eng["x"], ora["x"], rtol=1e-3, atol=2e-5)
+
+
+def test_lactotroph_nhood2_per_member_tspan():
+    n = 512
+    rng = np.random.default_rng(SEED)
+    gcal = rng.uniform(0.5, 3.0, n)
+    gbk = rng.uniform(0.0, 2.0, n)
+    pars = np.stack([gcal, np.full(n, 3.0), gbk], axis=1)
+    x0 = np.tile([-60.0, 0.0, 0.0, 0.1], (n, 1))
+    t1 = rng.uniform(1e3, 3e3, n)
+    tspan = np.stack([np.zeros(n), t1], axis=1)
+    sc = Scenario("lactotroph.cl", 4, 3, x0, pars, n_aux=1, stepper="dopri5", observer="nhood2", single=True,
+                  sp=dict(dt=0.1, dtmax=100.0, abstol=1e-6, reltol=1e-6, max_steps=10000000),
+                  op=dict(e_var_ix=3, f_var_ix=0, max_event_count=100000, nhood_radius=0.05,
+                          x_down_threshold=0.2), tspan_pm=tspan,
+                  steps=[("features",)])
+    eng, ora = run_engine(sc), run_oracle(sc)
+    F, G = eng["F_list"][0], ora["F_list"][0]
+    names = eng["feature_names"]
+    assert len(names) == 42
+    np.testing.assert_allclose(eng["tf"], ora["tf"], rtol=1e-5)
+    ev = names.index("event count")
+    # tolerance: exp/pow ulp differences; spike counts exact for >= 97% of members
+    assert np.mean(F[:, ev] == G[:, ev]) >= 0.97
+    pk = names.index("mean peaks")
+    assert np.mean(np.isclose(F[:, pk], G[:, pk], rtol=1e-3, atol=1e-3)) >= 0.95
+
+
+@pytest.mark.parametrize("fuse", [0, 1])
+def test_observer_initialisation_fused_or_separate(fuse):
+    x0, p = lorenz_inputs(128)
+    sc = Scenario("lorenz.cl", 3, 3, x0, p, n_aux=1, stepper="rk4", observer="thresh2", single=False,
+                  sp=dict(dt=0.005, max_steps=100000),
+                  op=dict(e_var_ix=2, f_var_ix=2, max_event_count=10000, x_up_threshold=0.3, x_down_threshold=0.2),
+                  steps=[("features", (0.0, 10.0)), ("features", (0.0, 10.0), True), ("initialize_observer", None),
+                         ("features", None)])
+    eng, ora = run_engine(sc, options={"fuse_init": fuse}), run_oracle(sc)
+    assert_bitwise(eng, ora)
