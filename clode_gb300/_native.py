@@ -117,6 +117,8 @@ SIGNATURES = {
     "clode_sim_get_string": (C.c_int, [_P, C.c_int, C.c_char_p, _SIZE, C.POINTER(_SIZE)]),
     "clode_sim_set_tspan_per_member": (C.c_int, [_P, _DP, _SIZE]),
     "clode_sim_get_status": (C.c_int, [_P, C.POINTER(C.c_int), _SIZE, C.POINTER(_SIZE)]),
+    "clode_sim_get_rng_state": (C.c_int, [_P, C.POINTER(C.c_ulonglong), _SIZE, C.POINTER(_SIZE)]),
+    "clode_sim_set_rng_state": (C.c_int, [_P, C.POINTER(C.c_ulonglong), _SIZE]),
     "clode_sim_get_stats": (C.c_int, [_P, C.POINTER(C.c_ulonglong)]),
     "clode_sim_last_kernel_ms": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "clode_sim_set_option": (C.c_int, [_P, C.c_char_p, C.c_double]),

@@ -592,6 +592,21 @@ class SimulatorBase:
                                               C.byref(n)))
         return out
 
+    def get_rng_state(self) -> np.ndarray:
+        """Raw RNG state, 2*nPts uint64 words laid out [j*nPts + i] (no reference counterpart)."""
+        n = C.c_size_t(0)
+        _check(N.lib.clode_sim_get_rng_state(self._handle, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.uint64)
+        if n.value:
+            _check(N.lib.clode_sim_get_rng_state(self._handle, out.ctypes.data_as(C.POINTER(C.c_ulonglong)),
+                                                 out.size, C.byref(n)))
+        return out
+
+    def set_rng_state(self, state) -> None:
+        """Set the raw RNG state (2*nPts uint64 words, layout [j*nPts + i])."""
+        a = np.ascontiguousarray(np.asarray(state, dtype=np.uint64).ravel())
+        _check(N.lib.clode_sim_set_rng_state(self._handle, a.ctypes.data_as(C.POINTER(C.c_ulonglong)), a.size))
+
     def get_stats(self) -> dict:
         """Launch-wide counters of the last run: steps, rejected, rhs_evals, events."""
         buf = (C.c_ulonglong * N.STAT_COUNT)()

@@ -130,6 +130,34 @@ __device__ __forceinline__ void flush_counters(const Args &a, const Counters &c)
     }
 }
 
+// ------------------------------------------------------------ scheduling --
+// Persistent schedule: hand out the next members of [i_begin, i_end) to the
+// lanes of this warp that ask for one, with a single atomic per warp.  Every
+// lane of the warp must call it (full-mask vote); lanes with want == false
+// get -1.  Returns -1 as well once the range is exhausted.
+__device__ __forceinline__ int fetch_member(const Args &a, bool want)
+{
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned int mask = __ballot_sync(0xffffffffu, want);
+    if (mask == 0u)
+        return -1;
+    const unsigned int leader = __ffs(mask) - 1;
+    unsigned int base = 0;
+    if (lane == leader)
+        base = atomicAdd(a.work_next, (unsigned int)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!want)
+        return -1;
+    long long k = (long long)a.i_begin + base + __popc(mask & ((1u << lane) - 1u));
+    return k < a.i_end ? (int)k : -1;
+}
+
+// true when this lane should stop taking new members (time budget spent)
+__device__ __forceinline__ bool budget_spent(const Args &a, unsigned long long t_start)
+{
+    return a.time_budget_ns != 0ull && globaltimer_ns() - t_start > a.time_budget_ns;
+}
+
 // ------------------------------------------------------------- transient --
 __device__ __forceinline__ void run_transient(const Args &a, int i, Counters &c)
 {
@@ -153,6 +181,52 @@ extern "C" __global__ void clode_transient(const Args a)
     int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.i_end)
         run_transient(a, i, c);
+    flush_counters(a, c);
+}
+
+// transient, persistent schedule: each lane refills itself as its member ends
+extern "C" __global__ void clode_transient_persistent(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    const unsigned long long t_start = globaltimer_ns();
+    bool exhausted = false;
+    int i = -1;
+    unsigned int step = 0;
+    bool hmin_fail = false;
+    realtype t1 = ZERO;
+    Member m;
+    for (;;) {
+        bool want = i < 0 && !exhausted;
+        if (want && budget_spent(a, t_start)) {
+            want = false;
+            exhausted = true;
+        }
+        int got = fetch_member(a, want);
+        if (want) {
+            if (got < 0) {
+                exhausted = true;
+            } else {
+                i = got;
+                step = 0;
+                hmin_fail = false;
+                member_load(m, a, i, c);
+                t1 = member_t1(a, i);
+            }
+        }
+        if (__all_sync(0xffffffffu, i < 0))
+            break;
+        if (i < 0)
+            continue;
+        if (m.t <= t1 && step < a.sp.max_steps) {
+            ++step;
+            hmin_fail |= step_member(m, a.sp, t1, c) != 0;
+        } else {
+            member_store(m, a, i);
+            if (a.status)
+                a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, false);
+            i = -1;
+        }
+    }
     flush_counters(a, c);
 }
 
@@ -201,6 +275,60 @@ extern "C" __global__ void clode_trajectory(const Args a)
     int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.i_end)
         run_trajectory(a, i, c);
+    flush_counters(a, c);
+}
+
+// trajectory, persistent schedule
+extern "C" __global__ void clode_trajectory_persistent(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    const unsigned long long t_start = globaltimer_ns();
+    bool exhausted = false;
+    int i = -1;
+    unsigned int step = 0;
+    unsigned long long row = 0;
+    bool hmin_fail = false;
+    realtype t1 = ZERO;
+    Member m;
+    for (;;) {
+        bool want = i < 0 && !exhausted;
+        if (want && budget_spent(a, t_start)) {
+            want = false;
+            exhausted = true;
+        }
+        int got = fetch_member(a, want);
+        if (want) {
+            if (got < 0) {
+                exhausted = true;
+            } else {
+                i = got;
+                step = 0;
+                row = 0;
+                hmin_fail = false;
+                member_load(m, a, i, c);
+                t1 = member_t1(a, i);
+                store_row(a, m, i, row);
+            }
+        }
+        if (__all_sync(0xffffffffu, i < 0))
+            break;
+        if (i < 0)
+            continue;
+        if (m.t <= t1 && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store) {
+            ++step;
+            hmin_fail |= step_member(m, a.sp, t1, c) != 0;
+            if (step % a.sp.nout == 0) {
+                ++row;
+                store_row(a, m, i, row);
+            }
+        } else {
+            a.n_stored[i] = (int)row;
+            member_store(m, a, i);
+            if (a.status)
+                a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, false);
+            i = -1;
+        }
+    }
     flush_counters(a, c);
 }
 
@@ -309,6 +437,101 @@ extern "C" __global__ void clode_features(const Args a)
             park_load(o, a, i);
         features_member(o, a, i, c);
         park_store(o, a, i);
+    }
+    flush_counters(a, c);
+}
+
+// Features, persistent schedule.  A lane walks its member through the
+// observer's warm-up pass (two-pass observers, when the initialisation is
+// fused into this launch) and the feature pass, then takes the next member.
+// Both passes go through the same step_member call, so lanes in different
+// passes stay converged on the expensive part of the loop.
+extern "C" __global__ void clode_features_persistent(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    const unsigned long long t_start = globaltimer_ns();
+    bool exhausted = false;
+    int i = -1;
+    bool warm = false;  // in the warm-up pass
+    unsigned int step = 0;
+    bool hmin_fail = false, terminal = false;
+    realtype t0 = ZERO, t1 = ZERO;
+    Member m;
+    Observer o;
+    for (;;) {
+        bool want = i < 0 && !exhausted;
+        if (want && budget_spent(a, t_start)) {
+            want = false;
+            exhausted = true;
+        }
+        int got = fetch_member(a, want);
+        if (want) {
+            if (got < 0) {
+                exhausted = true;
+            } else {
+                i = got;
+                step = 0;
+                hmin_fail = false;
+                terminal = false;
+                member_load(m, a, i, c);
+                t0 = m.t;
+                t1 = member_t1(a, i);
+                if (a.fused_init) {
+                    o.init(m.t, m.x, m.dx, m.aux, a.op);
+                    warm = Observer::two_pass;
+                    if (!warm)  // one-pass: arm on the initial state, the feature pass starts from it
+                        o.arm(m.t, m.x, m.dx, m.aux, a.op);
+                } else {
+                    park_load(o, a, i);
+                    warm = false;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, i < 0))
+            break;
+        if (i < 0)
+            continue;
+        bool running = step < a.sp.max_steps && (warm ? m.t < t1 : m.t <= t1);
+        if (running) {
+            ++step;
+            int flag = step_member(m, a.sp, t1, c);
+            if (warm) {
+                o.warmup(m.t, m.x, m.dx, m.aux, a.op);
+            } else {
+                hmin_fail |= flag != 0;
+                o.update(m.t, m.x, m.dx, m.aux, a.op);
+                if (o.event(m.t, m.x, m.dx, m.aux, a.op)) {
+                    c.events++;
+                    if (o.on_event(m.t, m.x, m.dx, m.aux, a.op)) {
+                        terminal = true;
+                        running = false;
+                    }
+                }
+            }
+        }
+        if (!running) {
+            if (warm) {
+                // end of the warm-up pass: rewind (keeping the last noise
+                // sample), arm the detector, restart from the stored state
+                m.t = t0;
+                load_x0(m.x, a, i);
+                getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
+                c.rhs += 1;
+                o.arm(m.t, m.x, m.dx, m.aux, a.op);
+                member_load(m, a, i, c);
+                warm = false;
+                step = 0;
+            } else {
+                FOut out = {a.F, (unsigned long long)a.nPts, i, 0};
+                o.write(out);
+                o.rebase(m.t - t0);
+                member_store(m, a, i);
+                park_store(o, a, i);
+                if (a.status)
+                    a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, terminal);
+                i = -1;
+            }
+        }
     }
     flush_counters(a, c);
 }

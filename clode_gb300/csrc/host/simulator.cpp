@@ -198,6 +198,8 @@ struct clode_sim {
     cudaLibrary_t lib = nullptr;
     int lib_device = -1;
     cudaKernel_t k_transient = nullptr, k_trajectory = nullptr, k_init = nullptr, k_features = nullptr;
+    cudaKernel_t kp_transient = nullptr, kp_trajectory = nullptr, kp_features = nullptr;
+    int last_grid = 0, last_block = 0;
     unsigned int obs_words = 0;
     unsigned int built_nse = 0;
 
@@ -362,11 +364,17 @@ struct clode_sim {
             lib_device = device;
             check_cuda(cudaLibraryGetKernel(&k_transient, lib, "clode_transient"), "kernel clode_transient");
             check_cuda(cudaLibraryGetKernel(&k_trajectory, lib, "clode_trajectory"), "kernel clode_trajectory");
-            k_init = k_features = nullptr;
+            check_cuda(cudaLibraryGetKernel(&kp_transient, lib, "clode_transient_persistent"),
+                       "kernel clode_transient_persistent");
+            check_cuda(cudaLibraryGetKernel(&kp_trajectory, lib, "clode_trajectory_persistent"),
+                       "kernel clode_trajectory_persistent");
+            k_init = k_features = kp_features = nullptr;
             obs_words = 0;
             if (kind == CLODE_SIM_FEATURES) {
                 check_cuda(cudaLibraryGetKernel(&k_init, lib, "clode_init_observer"), "kernel clode_init_observer");
                 check_cuda(cudaLibraryGetKernel(&k_features, lib, "clode_features"), "kernel clode_features");
+                check_cuda(cudaLibraryGetKernel(&kp_features, lib, "clode_features_persistent"),
+                           "kernel clode_features_persistent");
                 void *gp = nullptr;
                 size_t gb = 0;
                 check_cuda(cudaLibraryGetGlobal(&gp, &gb, lib, "clode_observer_words"), "observer state size");
@@ -574,12 +582,34 @@ struct clode_sim {
         return a;
     }
 
-    void launch(cudaKernel_t k, int fused_init)
+    // grid schedule: one thread per member.  persistent schedule: as many
+    // resident blocks as the SMs hold (or blocks_per_sm per SM), lanes pull
+    // members from a counter; never more threads than members.
+    void launch(cudaKernel_t kgrid, cudaKernel_t kpersist, int fused_init)
     {
         if (nPts == 0)
             return;
         unsigned int block = (unsigned int)std::max(32, std::min(1024, block_size));
         unsigned int grid = (unsigned int)((nPts + block - 1) / block);
+        cudaKernel_t k = kgrid;
+        if (schedule == 1 && kpersist) {
+            k = kpersist;
+            int per_sm = blocks_per_sm;
+            if (per_sm <= 0) {
+                check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k, (int)block, 0),
+                           "occupancy query");
+                per_sm = std::max(per_sm, 1);
+            }
+            int sms = 0;
+            check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count");
+            unsigned long long want = (unsigned long long)per_sm * sms;
+            grid = (unsigned int)std::min<unsigned long long>(want, grid);
+            check_cuda(cudaMemsetAsync(work.p, 0, sizeof(unsigned int), stream), "work counter reset");
+            if (time_budget_ms > 0.0)
+                launch_fill_i32(status.as<int>(), STATUS_TIME_BUDGET, (size_t)nPts, stream);
+        }
+        last_grid = (int)grid;
+        last_block = (int)block;
         if (single) {
             ArgsT<float> a = make_args<float>();
             a.fused_init = fused_init;
@@ -634,7 +664,7 @@ struct clode_sim {
     {
         require_problem();
         begin_run();
-        launch(k_transient, 0);
+        launch(k_transient, kp_transient, 0);
         end_run("transient");
         log_msg(CLODE_LOG_INFO, "run transient");
     }
@@ -661,7 +691,7 @@ struct clode_sim {
             fail(CLODE_ERR_STATE, "not a feature simulator");
         begin_run();
         resize_features();
-        launch(k_init, 0);
+        launch(k_init, nullptr, 0);
         end_run("initializeObserver");
         observer_initialized = true;
         log_msg(CLODE_LOG_DEBUG, "run initializeObserver");
@@ -687,7 +717,7 @@ struct clode_sim {
             }
         }
         begin_run();
-        launch(k_features, fused);
+        launch(k_features, kp_features, fused);
         end_run("features");
         last_ms += init_ms;
         observer_initialized = true;
@@ -730,7 +760,7 @@ struct clode_sim {
         ensure_stream();
         resize_trajectory();
         begin_run();
-        launch(k_trajectory, 0);
+        launch(k_trajectory, kp_trajectory, 0);
         end_run("trajectory");
         log_msg(CLODE_LOG_DEBUG, "run trajectory");
     }
@@ -1157,6 +1187,32 @@ int clode_sim_get_status(clode_sim *sim, int *out, size_t capacity, size_t *n)
     });
 }
 
+int clode_sim_get_rng_state(clode_sim *sim, unsigned long long *out, size_t capacity, size_t *n)
+{
+    SIM_GUARD({
+        size_t len = sim->nPts > 0 ? 2 * (size_t)sim->nPts : 0;
+        if (n)
+            *n = len;
+        if (!out || !len)
+            return;
+        if (capacity < len)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "output capacity %zu is smaller than 2*nPts (%zu)", capacity, len);
+        sim->ensure_stream();
+        check_cuda(cudaMemcpy(out, sim->rng.p, len * sizeof(unsigned long long), cudaMemcpyDeviceToHost), "D2H copy");
+    });
+}
+
+int clode_sim_set_rng_state(clode_sim *sim, const unsigned long long *state, size_t n)
+{
+    SIM_GUARD({
+        if (sim->nPts <= 0 || n != 2 * (size_t)sim->nPts)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "RNG state needs 2*nPts=%lld words, received %zu", 2 * sim->nPts, n);
+        need(state, "state");
+        sim->ensure_stream();
+        check_cuda(cudaMemcpy(sim->rng.p, state, n * sizeof(unsigned long long), cudaMemcpyHostToDevice), "H2D copy");
+    });
+}
+
 int clode_sim_get_stats(clode_sim *sim, unsigned long long *out)
 {
     SIM_GUARD({
@@ -1250,6 +1306,8 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "time_budget_ms") *value = sim->time_budget_ms;
         else if (k == "fuse_init") *value = sim->fuse_init;
         else if (k == "collect_stats") *value = sim->collect_stats;
+        else if (k == "last_grid") *value = sim->last_grid;
+        else if (k == "last_block") *value = sim->last_block;
         else fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);
     });
 }
@@ -1263,7 +1321,10 @@ int clode_sim_kernel_info(clode_sim *sim, const char *kernel, int *registers, in
         cudaKernel_t kk = k == "transient" ? sim->k_transient
                           : k == "trajectory" ? sim->k_trajectory
                           : k == "init_observer" ? sim->k_init
-                          : k == "features" ? sim->k_features : nullptr;
+                          : k == "features" ? sim->k_features
+                          : k == "transient_persistent" ? sim->kp_transient
+                          : k == "trajectory_persistent" ? sim->kp_trajectory
+                          : k == "features_persistent" ? sim->kp_features : nullptr;
         if (!kk)
             fail(CLODE_ERR_INVALID_ARGUMENT, "no kernel '%s' in this program", kernel);
         cudaFuncAttributes fa;

@@ -220,6 +220,11 @@ int clode_sim_get_string(clode_sim *sim, int which, char *buf, size_t capacity, 
 /* Per-member time spans: tspan[2*i], tspan[2*i+1] for member i (n = 2*nPts).
  * Replaces the single global tspan until clode_sim_set_tspan() is called again. */
 int clode_sim_set_tspan_per_member(clode_sim *sim, const double *tspan, size_t n);
+/* Raw per-member RNG state: 2*nPts u64 words laid out [j*nPts + i] as the
+ * kernels read it (clode/cpp/transient.cl:37-39).  Setting it lets a shard of a
+ * larger ensemble continue exactly the streams the full ensemble would use. */
+int clode_sim_get_rng_state(clode_sim *sim, unsigned long long *out, size_t capacity, size_t *n);
+int clode_sim_set_rng_state(clode_sim *sim, const unsigned long long *state, size_t n);
 /* Per-member status bits of the last run (CLODE_MEMBER_*). */
 int clode_sim_get_status(clode_sim *sim, int *out, size_t capacity, size_t *n);
 /* Launch-wide counters of the last run (CLODE_STAT_*; out has CLODE_STAT_COUNT slots). */

@@ -63,8 +63,10 @@ def _collect(out: dict, get_xf, get_tf, get_dt):
     out["dt"] = get_dt()
 
 
-def run_oracle(sc: Scenario, nthreads: int | None = None) -> dict:
-    s = OracleSimulator(sc.oracle_config(), nthreads=nthreads)
+def run_oracle(sc: Scenario, nthreads: int | None = None, reference: bool = False) -> dict:
+    """Run the scenario on the CPU: the C restatement, or (reference=True)
+    clODE's own kernels compiled as C, where the clODE sources exist."""
+    s = OracleSimulator(sc.oracle_config(), nthreads=nthreads, reference=reference)
     sp = dict(SP_DEFAULT, **sc.sp)
     s.set_solver_params(**sp)
     if sc.observer:

@@ -1,0 +1,170 @@
+"""C ABI checks that need no GPU: the library loads, exports every entry
+point include/clode_gb300.h declares, reports errors with the documented
+codes, and cross-compiles ensemble programs for sm_103a with NVRTC."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from clode_gb300 import _native as N, rhs_path
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "clode_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?(?:unsigned\s+long\s+long|int|const char)\s*\*?\s*(clode_\w+)\s*\(",
+                       text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_the_abi():
+    names = declared_functions()
+    assert len(names) >= 45
+    for must in ("clode_sim_create", "clode_sim_features", "clode_sim_trajectory", "clode_sim_transient",
+                 "clode_sim_get", "clode_last_error", "clode_device_query"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(N.library_path())
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the ctypes binding covers the whole header
+    assert set(declared_functions()) <= set(N.SIGNATURES)
+
+
+def test_version_and_device_count_without_gpu():
+    assert N.lib.clode_version() == 100
+    n = C.c_int(-1)
+    assert N.lib.clode_device_count(C.byref(n)) == 0
+    assert n.value >= 0
+
+
+def _problem(name="van_der_pol.cl", nv=2, np_=1, na=0, nw=0):
+    src = open(rhs_path(name)).read().encode()
+    keep = [src]
+    return N.CProblem(src, name.encode(), nv, np_, na, nw, b"x\ny", b"mu", b""), keep
+
+
+def test_create_rejects_unknown_stepper_and_observer():
+    cp, keep = _problem()
+    h = C.c_void_p()
+    rc = N.lib.clode_sim_create(N.SIM_BASE, C.byref(cp), b"rk5", None, None, 0, 0, C.byref(h))
+    assert rc == 1 and b"stepper" in N.lib.clode_last_error()
+    op = N.CObserverParams(0, 0, 100, 0, 0, 0, 0.05, 0.2, 0.2, 0, 0, 0)
+    rc = N.lib.clode_sim_create(N.SIM_FEATURES, C.byref(cp), b"rk4", b"nhood3", C.byref(op), 0, 0, C.byref(h))
+    assert rc == 1 and b"observer" in N.lib.clode_last_error()
+
+
+def test_runs_need_problem_data_and_report_state_errors():
+    cp, keep = _problem()
+    h = C.c_void_p()
+    N.check(N.lib.clode_sim_create(N.SIM_BASE, C.byref(cp), b"rk4", None, None, 0, 0, C.byref(h)))
+    try:
+        assert N.lib.clode_sim_transient(h) == 7  # CLODE_ERR_STATE
+        assert b"problem data" in N.lib.clode_last_error()
+        assert N.lib.clode_sim_features(h, -1) == 7
+        # setters that need nothing on the device
+        sp = N.CSolverParams(0.05, 1.0, 1e-7, 1e-5, 1000, 10, 2)
+        N.check(N.lib.clode_sim_set_solver_params(h, C.byref(sp)))
+        back = N.CSolverParams()
+        N.check(N.lib.clode_sim_get_solver_params(h, C.byref(back)))
+        assert (back.dt, back.max_store, back.nout) == (0.05, 10, 2)
+        # unknown option and an out-of-range one
+        assert N.lib.clode_sim_set_option(h, b"no_such_option", 1.0) == 1
+        assert N.lib.clode_sim_set_option(h, b"block_size", 7.0) == 1
+    finally:
+        N.lib.clode_sim_destroy(h)
+
+
+def test_strings_available_steppers_and_observers():
+    cp, keep = _problem("lorenz.cl", 3, 3, 1)
+    op = N.CObserverParams(2, 2, 100, 2, 0, 0, 0.05, 0.3, 0.2, 0, 0, 0)
+    h = C.c_void_p()
+    N.check(N.lib.clode_sim_create(N.SIM_FEATURES, C.byref(cp), b"dopri5", b"thresh2", C.byref(op), 1, 0, C.byref(h)))
+
+    def get(which):
+        n = C.c_size_t()
+        N.check(N.lib.clode_sim_get_string(h, which, None, 0, C.byref(n)))
+        b = C.create_string_buffer(n.value + 1)
+        N.check(N.lib.clode_sim_get_string(h, which, b, n.value + 1, C.byref(n)))
+        return b.value.decode()
+
+    try:
+        # std::map order of clode/cpp/steppers.cl:26-43 and observers.cl:122-143
+        assert get(N.STRING_AVAILABLE_STEPPERS).split("\n") == ["bs23", "dopri5", "euler", "heun", "rk4", "seuler"]
+        assert get(N.STRING_AVAILABLE_OBSERVERS).split("\n") == ["basic", "basicall", "localmax", "nhood1",
+                                                                  "nhood2", "thresh2"]
+        names = get(N.STRING_FEATURE_NAMES).split("\n")
+        # thresh2: 18 period stats + 5 per var + 3 per aux + 2 per stored event + 5 diagnostics
+        assert len(names) == 18 + 15 + 3 + 4 + 5
+        assert names[0] == "max period" and names[-1] == "mean dt"
+        assert "up event time 1" in names and "down event time 0" in names
+        assert get(N.STRING_OBSERVER_NAME) == "thresh2"
+    finally:
+        N.lib.clode_sim_destroy(h)
+
+
+@pytest.mark.parametrize("stepper,observer,single", [
+    ("euler", "basic", True), ("heun", "basicall", False), ("rk4", "localmax", True), ("bs23", "nhood1", False),
+    ("dopri5", "nhood2", True), ("seuler", "thresh2", True), ("dopri5", "thresh2", False),
+])
+def test_nvrtc_builds_for_sm103a_without_spills(stepper, observer, single):
+    cp, keep = _problem("lorenz.cl", 3, 3, 1, 1 if stepper == "seuler" else 0)
+    op = N.CObserverParams(2, 0, 100, 1, 0, 0, 0.05, 0.3, 0.2, 0, 0, 0)
+    h = C.c_void_p()
+    N.check(N.lib.clode_sim_create(N.SIM_FEATURES, C.byref(cp), stepper.encode(), observer.encode(), C.byref(op),
+                                   int(single), 0, C.byref(h)))
+    try:
+        N.check(N.lib.clode_sim_build(h))
+        n = C.c_size_t()
+        N.lib.clode_sim_get_string(h, N.STRING_BUILD_LOG, None, 0, C.byref(n))
+        b = C.create_string_buffer(n.value + 1)
+        N.lib.clode_sim_get_string(h, N.STRING_BUILD_LOG, b, n.value + 1, C.byref(n))
+        log = b.value.decode()
+        if log:  # empty when the program came from the on-disk cache of an earlier build without a log
+            assert "sm_103a" in log
+            for k in ("clode_features", "clode_init_observer", "clode_transient", "clode_trajectory"):
+                assert f"entry function '{k}'" in log
+            assert "bytes spill stores" in log
+            assert all(int(s) == 0 for s in re.findall(r"(\d+) bytes spill stores", log))
+            assert all(int(s) == 0 for s in re.findall(r"(\d+) bytes stack frame", log))
+    finally:
+        N.lib.clode_sim_destroy(h)
+
+
+def test_broken_model_source_reports_compile_error():
+    src = b"void getRHS(const realtype t, const realtype x_[], const realtype p_[], realtype dx_[], " \
+          b"realtype aux_[], const realtype w_[]) { dx_[0] = undefined_symbol * x_[0]; }"
+    cp = N.CProblem(src, b"broken.cl", 1, 0, 0, 0, b"x", b"", b"")
+    h = C.c_void_p()
+    N.check(N.lib.clode_sim_create(N.SIM_BASE, C.byref(cp), b"rk4", None, None, 1, 0, C.byref(h)))
+    try:
+        rc = N.lib.clode_sim_build(h)
+        assert rc == 3  # CLODE_ERR_COMPILE
+        assert b"undefined_symbol" in N.lib.clode_last_error()
+    finally:
+        N.lib.clode_sim_destroy(h)
+
+
+def test_log_levels_and_sink(capfd):
+    from clode_gb300 import clode_cpp_wrapper as W
+
+    lg = W.get_logger()
+    lg.set_log_level(W.LogLevel.trace)
+    assert lg.get_log_level() == W.LogLevel.trace
+    W._log(W.LogLevel.info, "hello from the engine log")
+    out = capfd.readouterr().out
+    assert "hello from the engine log" in out and "[info]" in out
+    lg.set_log_level(W.LogLevel.off)
+    W._log(W.LogLevel.critical, "silent")
+    out = capfd.readouterr()
+    assert out.out == "" and out.err == ""
+    lg.set_log_pattern("%l: %v")
+    lg.set_log_level(W.LogLevel.warn)
+    W._log(W.LogLevel.warn, "patterned")
+    assert capfd.readouterr().out.strip() == "warning: patterned"
+    lg.set_log_pattern("[%Y-%m-%d %H:%M:%S.%e] [%n] [%l] %v")
