@@ -65,7 +65,7 @@ def _write_device_headers() -> str:
 
 
 def _sources() -> list[str]:
-    return [os.path.join(HOST_DIR, fn) for fn in ("runtime.cpp", "simulator.cpp", "aot_kernels.cu")]
+    return [os.path.join(HOST_DIR, fn) for fn in ("runtime.cpp", "simulator.cpp", "aot_kernels.cu", "noalloc.cu")]
 
 
 def _fingerprint(flags: list[str]) -> str:
@@ -106,7 +106,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(r.stdout, r.stderr, file=sys.stderr)
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:
         objs = list(ex.map(compile_one, _sources()))
     tmp = lib + f".tmp{os.getpid()}"
     cmd = [nvcc, "-shared", "-cudart", "static"] + ARCH_FLAGS + objs + ["-o", tmp, "-ldl", "-lpthread", "-lrt"]

@@ -59,6 +59,27 @@ void set_cache_dir(const std::string &dir);
 // every kernel launch the library issues is counted (clode_launch_count)
 void count_launch();
 
+// Launch description of a built feature simulator's persistent features
+// kernel, for the entry point that allocates nothing (noalloc.cu): solver and
+// observer parameters and the global time span filled in, every buffer
+// pointer left null for the caller's memory and the shared scratch.
+struct NoallocFeaturesLaunch {
+    void *kernel;          // cudaKernel_t of clode_features_persistent
+    int single;            // working precision is float
+    unsigned int obs_words;
+    int device;
+    int block;
+    unsigned char args[512];  // ArgsT<float> or ArgsT<double>
+};
+}  // namespace clode
+
+struct clode_sim;
+
+namespace clode {
+void noalloc_features_prepare(clode_sim *sim, NoallocFeaturesLaunch *out);
+// sets the message clode_last_error() returns on this thread
+void set_last_error_message(const char *msg);
+
 // -------------------------------------------------------------- AOT kernels
 void launch_f64_to_f32(const double *src, float *dst, size_t n, cudaStream_t s);
 void launch_f32_to_f64(const float *src, double *dst, size_t n, cudaStream_t s);

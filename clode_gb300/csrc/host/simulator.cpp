@@ -1337,3 +1337,49 @@ int clode_sim_kernel_info(clode_sim *sim, const char *kernel, int *registers, in
 }
 
 }  // extern "C"
+
+// ------------------------------------------ for the no-allocation entry point
+namespace clode {
+
+static_assert(sizeof(ArgsT<double>) <= sizeof(((NoallocFeaturesLaunch *)nullptr)->args), "argument block size");
+
+void set_last_error_message(const char *msg) { g_last_error = msg ? msg : ""; }
+
+void noalloc_features_prepare(clode_sim *sim, NoallocFeaturesLaunch *out)
+{
+    if (!sim)
+        fail(CLODE_ERR_INVALID_ARGUMENT, "sim must not be NULL");
+    if (sim->kind != CLODE_SIM_FEATURES)
+        fail(CLODE_ERR_STATE, "not a feature simulator");
+    if (!sim->built || !sim->lib || !sim->kp_features)
+        fail(CLODE_ERR_NOT_BUILT, "the feature simulator must be built (clode_sim_build) on its device first");
+    if (sim->built_nse != sim->op.max_event_timestamps)
+        fail(CLODE_ERR_NOT_BUILT, "observer parameters changed the program: rebuild with clode_sim_build");
+    memset(out, 0, sizeof *out);
+    out->kernel = (void *)sim->kp_features;
+    out->single = sim->single ? 1 : 0;
+    out->obs_words = sim->obs_words;
+    out->device = sim->lib_device;
+    out->block = std::max(32, std::min(1024, sim->block_size));
+    if (sim->single) {
+        ArgsT<float> a = sim->make_args<float>();
+        ArgsT<float> clean;
+        memset(&clean, 0, sizeof clean);
+        clean.t0 = a.t0;
+        clean.t1 = a.t1;
+        clean.sp = a.sp;
+        clean.op = a.op;
+        memcpy(out->args, &clean, sizeof clean);
+    } else {
+        ArgsT<double> a = sim->make_args<double>();
+        ArgsT<double> clean;
+        memset(&clean, 0, sizeof clean);
+        clean.t0 = a.t0;
+        clean.t1 = a.t1;
+        clean.sp = a.sp;
+        clean.op = a.op;
+        memcpy(out->args, &clean, sizeof clean);
+    }
+}
+
+}  // namespace clode
