@@ -127,6 +127,22 @@ SIGNATURES = {
     "clode_launch_count": (C.c_ulonglong, []),
     "clode_sim_features_noalloc": (C.c_int, [_P, C.c_longlong, _P, _P, _P, C.POINTER(C.c_ulonglong), _P, _P, _P,
                                              _P, C.POINTER(C.c_int), _P]),
+    "clode_sim_autotune": (C.c_int, [_P, C.c_longlong, C.POINTER(C.c_double)]),
+    "clode_sim_chain": (C.c_int, [_P, C.POINTER(C.c_int), C.c_int, C.c_int]),
+    "clode_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(_P)]),
+    "clode_mlp_destroy": (C.c_int, [_P]),
+    "clode_mlp_param_count": (C.c_int, [_P, C.POINTER(_SIZE)]),
+    "clode_mlp_get_params": (C.c_int, [_P, C.POINTER(C.c_float), _SIZE]),
+    "clode_mlp_set_params": (C.c_int, [_P, C.POINTER(C.c_float), _SIZE]),
+    "clode_mlp_gradients": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int,
+                                      C.POINTER(C.c_float), _SIZE, C.POINTER(C.c_float)]),
+    "clode_mlp_train": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_longlong, C.c_int, C.c_int,
+                                  C.c_float, C.c_ulonglong, C.POINTER(C.c_float)]),
+    "clode_mlp_predict": (C.c_int, [_P, C.POINTER(C.c_float), C.c_longlong, C.POINTER(C.c_float),
+                                    C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "clode_mlp_screen": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.POINTER(C.c_int)]),
+    "clode_mlp_timings": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 
 

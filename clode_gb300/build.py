@@ -65,12 +65,14 @@ def _write_device_headers() -> str:
 
 
 def _sources() -> list[str]:
-    return [os.path.join(HOST_DIR, fn) for fn in ("runtime.cpp", "simulator.cpp", "aot_kernels.cu", "noalloc.cu")]
+    return [os.path.join(HOST_DIR, fn) for fn in ("runtime.cpp", "simulator.cpp", "aot_kernels.cu", "noalloc.cu",
+                                                  "mlp.cu", "mlp_net.cpp")]
 
 
 def _fingerprint(flags: list[str]) -> str:
     h = hashlib.sha256(" ".join(flags).encode())
-    files = _sources() + [os.path.join(HOST_DIR, "common.hpp"), os.path.join(HERE, "..", "include", "clode_gb300.h")]
+    files = _sources() + [os.path.join(HOST_DIR, "common.hpp"), os.path.join(HOST_DIR, "mlp.hpp"),
+                          os.path.join(HERE, "..", "include", "clode_gb300.h")]
     files += [os.path.join(DEVICE_DIR, n) for n in device_header_files()]
     for fn in files:
         with open(fn, "rb") as f:
@@ -106,7 +108,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(r.stdout, r.stderr, file=sys.stderr)
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=4) as ex:
+    with cf.ThreadPoolExecutor(max_workers=6) as ex:
         objs = list(ex.map(compile_one, _sources()))
     tmp = lib + f".tmp{os.getpid()}"
     cmd = [nvcc, "-shared", "-cudart", "static"] + ARCH_FLAGS + objs + ["-o", tmp, "-ldl", "-lpthread", "-lrt"]

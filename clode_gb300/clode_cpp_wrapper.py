@@ -627,6 +627,22 @@ class SimulatorBase:
         _check(N.lib.clode_sim_get_option(self._handle, key.encode(), C.byref(v)))
         return v.value
 
+    CHAIN_OPS = {"transient": 0, "features": 1, "trajectory": 2, "shift_x0": 3}
+
+    def run_chain(self, ops, use_graph: bool = True) -> None:
+        """Run ops such as ["transient", "shift_x0", "features"] back to back,
+        captured as a CUDA graph and replayed (no reference counterpart)."""
+        codes = (C.c_int * len(ops))(*[self.CHAIN_OPS[o] for o in ops])
+        _check(N.lib.clode_sim_chain(self._handle, codes, len(ops), int(bool(use_graph))))
+
+    def autotune(self, sample: int = 0) -> dict:
+        """Pick register cap and block size by timing the persistent kernel on
+        members [0, sample) (no reference counterpart)."""
+        ms = C.c_double(0.0)
+        _check(N.lib.clode_sim_autotune(self._handle, int(sample), C.byref(ms)))
+        return {"ms": ms.value, "maxrregcount": int(self.get_option("maxrregcount")),
+                "block_size": int(self.get_option("block_size"))}
+
     def kernel_registers(self, kernel: str) -> int:
         r, t = C.c_int(0), C.c_int(0)
         _check(N.lib.clode_sim_kernel_info(self._handle, kernel.encode(), C.byref(r), C.byref(t)))

@@ -452,7 +452,9 @@ extern "C" __global__ void clode_features_persistent(const Args a)
     const unsigned long long t_start = globaltimer_ns();
     bool exhausted = false;
     int i = -1;
-    bool warm = false;  // in the warm-up pass
+    bool warm = false;    // in the warm-up pass
+    bool fresh = false;   // a new member to load
+    bool rewind = false;  // warm-up pass ended: reload the member for the feature pass
     unsigned int step = 0;
     bool hmin_fail = false, terminal = false;
     realtype t0 = ZERO, t1 = ZERO;
@@ -470,10 +472,21 @@ extern "C" __global__ void clode_features_persistent(const Args a)
                 exhausted = true;
             } else {
                 i = got;
-                step = 0;
+                fresh = true;
+            }
+        }
+        if (__all_sync(0xffffffffu, i < 0))
+            break;
+        if (i < 0)
+            continue;
+        // one load site for both a new member and the start of its feature
+        // pass, so the right-hand side is inlined here once
+        if (fresh || rewind) {
+            member_load(m, a, i, c);
+            step = 0;
+            if (fresh) {
                 hmin_fail = false;
                 terminal = false;
-                member_load(m, a, i, c);
                 t0 = m.t;
                 t1 = member_t1(a, i);
                 if (a.fused_init) {
@@ -485,12 +498,15 @@ extern "C" __global__ void clode_features_persistent(const Args a)
                     park_load(o, a, i);
                     warm = false;
                 }
+            } else {
+                // end of the warm-up pass: arm the detector on the initial
+                // state (the arm hooks read the state, not its slope), then
+                // run the feature pass from the stored state
+                o.arm(m.t, m.x, m.dx, m.aux, a.op);
+                warm = false;
             }
+            fresh = rewind = false;
         }
-        if (__all_sync(0xffffffffu, i < 0))
-            break;
-        if (i < 0)
-            continue;
         bool running = step < a.sp.max_steps && (warm ? m.t < t1 : m.t <= t1);
         if (running) {
             ++step;
@@ -511,16 +527,7 @@ extern "C" __global__ void clode_features_persistent(const Args a)
         }
         if (!running) {
             if (warm) {
-                // end of the warm-up pass: rewind (keeping the last noise
-                // sample), arm the detector, restart from the stored state
-                m.t = t0;
-                load_x0(m.x, a, i);
-                getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
-                c.rhs += 1;
-                o.arm(m.t, m.x, m.dx, m.aux, a.op);
-                member_load(m, a, i, c);
-                warm = false;
-                step = 0;
+                rewind = true;
             } else {
                 FOut out = {a.F, (unsigned long long)a.nPts, i, 0};
                 o.write(out);

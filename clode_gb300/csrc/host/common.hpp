@@ -39,6 +39,9 @@ struct ProgramSpec {
     std::string rhs_name;
     std::vector<std::string> defines;   // "-DNAME=VALUE"
     bool fmad = false;
+    bool prec_div = true;               // IEEE division; false: approximate (2 ulp)
+    bool ftz = false;                   // flush FP32 denormals to zero
+    int maxrregcount = 0;               // 0: no register cap
     std::string arch;                   // e.g. "sm_103a"
 };
 

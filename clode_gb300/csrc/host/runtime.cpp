@@ -290,6 +290,12 @@ CompiledProgram compile_program(const ProgramSpec &spec)
     std::vector<std::string> opts = {"--gpu-architecture=" + spec.arch, "-default-device",
                                      std::string("--fmad=") + (spec.fmad ? "true" : "false"), "-std=c++17",
                                      "-lineinfo", "--ptxas-options=-v"};
+    if (!spec.prec_div)
+        opts.push_back("-prec-div=false");
+    if (spec.ftz)
+        opts.push_back("-ftz=true");
+    if (spec.maxrregcount > 0)
+        opts.push_back("--maxrregcount=" + std::to_string(spec.maxrregcount));
     for (auto &d : spec.defines)
         opts.push_back(d);
     std::string optline;

@@ -215,9 +215,13 @@ struct clode_sim {
     int block_size = 128;
     int blocks_per_sm = 0;
     bool fmad = false;
+    bool prec_div = true;
+    bool ftz = false;
+    int maxrregcount = 0;
     double time_budget_ms = 0.0;
     bool fuse_init = true;
     bool collect_stats = true;
+    long long range_end = -1;  // autotuner trials: run members [0, range_end) only
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -230,6 +234,8 @@ struct clode_sim {
             cudaSetDevice(buffers_device >= 0 ? buffers_device : lib_device);
             for (DevBuf *b : all_buffers())
                 b->release();
+            if (chain_graph)
+                cudaGraphExecDestroy(chain_graph);
             if (lib)
                 cudaLibraryUnload(lib);
             if (stream)
@@ -323,6 +329,9 @@ struct clode_sim {
         s.rhs_source = rhs_source;
         s.rhs_name = rhs_name;
         s.fmad = fmad;
+        s.prec_div = prec_div;
+        s.ftz = ftz;
+        s.maxrregcount = maxrregcount;
         s.arch = device_arch(device);
         s.defines = {single ? "-DCLODE_SINGLE_PRECISION" : "-DCLODE_DOUBLE_PRECISION", "-D" + kSteppers.at(stepper),
                      "-DN_PAR=" + std::to_string(nPar), "-DN_VAR=" + std::to_string(nVar),
@@ -539,7 +548,7 @@ struct clode_sim {
         memset(&a, 0, sizeof a);
         a.nPts = (int)nPts;
         a.i_begin = 0;
-        a.i_end = (int)nPts;
+        a.i_end = (int)(range_end >= 0 ? std::min(range_end, nPts) : nPts);
         a.t0 = (R)tspan[0];
         a.t1 = (R)tspan[1];
         a.tspan_pm = tspan_per_member ? tspan_dev.as<R>() : nullptr;
@@ -763,6 +772,197 @@ struct clode_sim {
         launch(k_trajectory, kp_trajectory, 0);
         end_run("trajectory");
         log_msg(CLODE_LOG_DEBUG, "run trajectory");
+    }
+
+    // Chains: a sequence of runs enqueued back to back on the stream with one
+    // synchronisation at the end, optionally captured once as a CUDA graph and
+    // replayed.  Each op behaves as the API call of the same name (the first
+    // features op of an uninitialised observer runs the initialisation in its
+    // launch).  A graph is re-captured when the ops, the ensemble, the time
+    // span, the options or the observer's initialisation state change.
+    cudaGraphExec_t chain_graph = nullptr;
+    std::string chain_key;
+    unsigned long long chain_kernels = 0;
+
+    void enqueue_op(int op, bool &obs_init)
+    {
+        switch (op) {
+        case CLODE_OP_TRANSIENT:
+            launch(k_transient, kp_transient, 0);
+            break;
+        case CLODE_OP_FEATURES:
+            if (kind != CLODE_SIM_FEATURES)
+                fail(CLODE_ERR_STATE, "features op on a simulator that is not a feature simulator");
+            launch(k_features, kp_features, obs_init ? 0 : 1);
+            obs_init = true;
+            break;
+        case CLODE_OP_TRAJECTORY:
+            if (sp.nout == 0)
+                fail(CLODE_ERR_INVALID_ARGUMENT, "solver parameter nout must be at least 1");
+            launch(k_trajectory, kp_trajectory, 0);
+            break;
+        case CLODE_OP_SHIFT_X0:
+            check_cuda(cudaMemcpyAsync(x0.p, xf.p, (size_t)nPts * nVar * real_size(), cudaMemcpyDeviceToDevice,
+                                       stream),
+                       "shift x0");
+            break;
+        default:
+            fail(CLODE_ERR_INVALID_ARGUMENT, "unknown chain op %d", op);
+        }
+    }
+
+    void chain(const int *ops, int n, bool use_graph)
+    {
+        require_problem();
+        ensure_built();
+        ensure_stream();
+        for (int k = 0; k < n; ++k) {  // every allocation happens before any capture
+            if (ops[k] == CLODE_OP_FEATURES && kind == CLODE_SIM_FEATURES)
+                resize_features();
+            if (ops[k] == CLODE_OP_TRAJECTORY)
+                resize_trajectory();
+        }
+        bool obs_init = observer_initialized;
+        if (collect_stats && nPts > 0)
+            check_cuda(cudaMemsetAsync(stats.p, 0, CLODE_STAT_COUNT * sizeof(unsigned long long), stream),
+                       "stats reset");
+        check_cuda(cudaEventRecord(ev0, stream), "event record");
+        if (use_graph) {
+            std::ostringstream key;
+            key << built_key << "|" << nPts << "|" << tspan[0] << "," << tspan[1] << "|" << tspan_per_member << "|"
+                << schedule << "," << block_size << "," << blocks_per_sm << "," << time_budget_ms << "|" << obs_init
+                << "|" << collect_stats << "|" << sp.dt << "," << sp.dtmax << "," << sp.abstol << "," << sp.reltol
+                << "," << sp.max_steps << "," << sp.max_store << "," << sp.nout << "|" << op.e_var_ix << ","
+                << op.f_var_ix << "," << op.max_event_count << "," << op.nhood_radius << "," << op.x_up_thresh << ","
+                << op.x_down_thresh << "," << op.dx_up_thresh << "," << op.dx_down_thresh << "," << op.min_x_amp
+                << "|";
+            for (int k = 0; k < n; ++k)
+                key << ops[k] << ",";
+            bool fresh_capture = !chain_graph || chain_key != key.str();
+            if (fresh_capture) {
+                if (chain_graph) {
+                    cudaGraphExecDestroy(chain_graph);
+                    chain_graph = nullptr;
+                }
+                unsigned long long before = clode_launch_count();
+                // capture between the two timing events: the graph holds the ops only
+                check_cuda(cudaStreamSynchronize(stream), "chain capture");
+                cudaGraph_t g;
+                check_cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed), "chain capture");
+                bool cap_init = obs_init;
+                try {
+                    for (int k = 0; k < n; ++k)
+                        enqueue_op(ops[k], cap_init);
+                } catch (...) {
+                    cudaStreamEndCapture(stream, &g);
+                    if (g)
+                        cudaGraphDestroy(g);
+                    throw;
+                }
+                check_cuda(cudaStreamEndCapture(stream, &g), "chain capture");
+                check_cuda(cudaGraphInstantiate(&chain_graph, g, 0), "chain graph instantiate");
+                cudaGraphDestroy(g);
+                chain_key = key.str();
+                // the kernels counted while capturing are the ones this first replay runs
+                chain_kernels = clode_launch_count() - before;
+            } else {
+                for (unsigned long long k = 0; k < chain_kernels; ++k)
+                    count_launch();
+            }
+            check_cuda(cudaGraphLaunch(chain_graph, stream), "chain graph launch");
+            for (int k = 0; k < n; ++k)
+                if (ops[k] == CLODE_OP_FEATURES)
+                    obs_init = true;
+        } else {
+            for (int k = 0; k < n; ++k)
+                enqueue_op(ops[k], obs_init);
+        }
+        end_run("chain");
+        observer_initialized = obs_init;
+    }
+
+    // Autotuner: for each (register cap, block size) candidate, build the
+    // program (later builds come from the on-disk cache) and time the
+    // persistent kernel of this simulator's kind on members [0, sample).
+    // The sampled members' dt and RNG words are restored after every trial;
+    // their other outputs are recomputed by the next run, and the observer is
+    // re-initialised.  Keeps the fastest candidate and the persistent schedule.
+    void autotune(long long sample, double *best_ms_out)
+    {
+        require_problem();
+        long long S = std::min(nPts, sample > 0 ? sample : nPts);
+        if (S <= 0)
+            fail(CLODE_ERR_STATE, "no members to tune on");
+        const int cands[][2] = {{0, 128}, {128, 128}, {96, 128}, {80, 128}, {64, 128}, {96, 64}, {80, 64}};
+        size_t rs = real_size();
+        DevBuf save_dt, save_rng;
+        save_dt.reserve((size_t)S * rs);
+        save_rng.reserve((size_t)S * 2 * sizeof(unsigned long long));
+        ensure_stream();
+        auto snapshot = [&](bool restore) {
+            auto cp = [&](void *dst, const void *src, size_t b) {
+                check_cuda(cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, stream), "autotune copy");
+            };
+            unsigned long long *r = rng.as<unsigned long long>(), *sr = save_rng.as<unsigned long long>();
+            if (!restore) {
+                cp(save_dt.p, dt.p, (size_t)S * rs);
+                cp(sr, r, (size_t)S * 8);
+                cp(sr + S, r + nPts, (size_t)S * 8);
+            } else {
+                cp(dt.p, save_dt.p, (size_t)S * rs);
+                cp(r, sr, (size_t)S * 8);
+                cp(r + nPts, sr + S, (size_t)S * 8);
+            }
+        };
+        snapshot(false);
+        double best = 1e300;
+        int best_regs = maxrregcount, best_block = block_size;
+        schedule = 1;
+        range_end = S;
+        try {
+            for (auto &cd : cands) {
+                if (maxrregcount != cd[0]) {
+                    maxrregcount = cd[0];
+                    built = false;
+                }
+                block_size = cd[1];
+                ensure_built();
+                if (kind == CLODE_SIM_FEATURES) {
+                    resize_features();
+                    begin_run();
+                    launch(k_features, kp_features, 1);
+                } else if (kind == CLODE_SIM_TRAJECTORY) {
+                    resize_trajectory();
+                    begin_run();
+                    launch(k_trajectory, kp_trajectory, 0);
+                } else {
+                    begin_run();
+                    launch(k_transient, kp_transient, 0);
+                }
+                end_run("autotune trial");
+                snapshot(true);
+                check_cuda(cudaStreamSynchronize(stream), "autotune restore");
+                log_msg(CLODE_LOG_INFO, "autotune: maxrregcount=%d block=%d: %.3f ms", cd[0], cd[1], last_ms);
+                if (last_ms < best) {
+                    best = last_ms;
+                    best_regs = cd[0];
+                    best_block = cd[1];
+                }
+            }
+        } catch (...) {
+            range_end = -1;
+            throw;
+        }
+        range_end = -1;
+        if (maxrregcount != best_regs) {
+            maxrregcount = best_regs;
+            built = false;
+        }
+        block_size = best_block;
+        observer_initialized = false;
+        ensure_built();
+        if (best_ms_out)
+            *best_ms_out = best;
     }
 
     void shift_x0()
@@ -1123,6 +1323,15 @@ int clode_sim_is_observer_initialized(clode_sim *sim, int *initialized)
     });
 }
 int clode_sim_trajectory(clode_sim *sim) { SIM_GUARD(sim->trajectory()); }
+int clode_sim_autotune(clode_sim *sim, long long sample, double *best_ms) { SIM_GUARD(sim->autotune(sample, best_ms)); }
+int clode_sim_chain(clode_sim *sim, const int *ops, int n_ops, int use_graph)
+{
+    SIM_GUARD({
+        if (n_ops < 0 || (n_ops > 0 && !ops))
+            fail(CLODE_ERR_INVALID_ARGUMENT, "invalid op list");
+        sim->chain(ops, n_ops, use_graph != 0);
+    });
+}
 int clode_sim_shift_tspan(clode_sim *sim) { SIM_GUARD(sim->shift_tspan()); }
 int clode_sim_shift_x0(clode_sim *sim) { SIM_GUARD(sim->shift_x0()); }
 
@@ -1281,6 +1490,21 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 sim->fmad = v;
                 sim->built = false;
             }
+        } else if (k == "prec_div" || k == "ftz") {
+            bool v = value != 0.0;
+            bool &field = k == "prec_div" ? sim->prec_div : sim->ftz;
+            if (v != field) {
+                field = v;
+                sim->built = false;
+            }
+        } else if (k == "maxrregcount") {
+            int v = (int)value;
+            if (v != 0 && (v < 32 || v > 255))
+                fail(CLODE_ERR_INVALID_ARGUMENT, "maxrregcount must be 0 or in [32, 255]");
+            if (v != sim->maxrregcount) {
+                sim->maxrregcount = v;
+                sim->built = false;
+            }
         } else if (k == "time_budget_ms") {
             sim->time_budget_ms = value;
         } else if (k == "fuse_init") {
@@ -1303,6 +1527,9 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "block_size") *value = sim->block_size;
         else if (k == "blocks_per_sm") *value = sim->blocks_per_sm;
         else if (k == "fmad") *value = sim->fmad;
+        else if (k == "prec_div") *value = sim->prec_div;
+        else if (k == "ftz") *value = sim->ftz;
+        else if (k == "maxrregcount") *value = sim->maxrregcount;
         else if (k == "time_budget_ms") *value = sim->time_budget_ms;
         else if (k == "fuse_init") *value = sim->fuse_init;
         else if (k == "collect_stats") *value = sim->collect_stats;

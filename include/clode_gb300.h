@@ -238,6 +238,19 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * "collect_stats" (0/1). */
 int clode_sim_set_option(clode_sim *sim, const char *key, double value);
 int clode_sim_get_option(clode_sim *sim, const char *key, double *value);
+/* Chains: ops run back to back on the simulator's stream, one synchronisation
+ * at the end; with use_graph the sequence is captured once as a CUDA graph and
+ * replayed while the ops, ensemble, time span, parameters and options stay the
+ * same.  Each op acts as its API call (a transient -> features chain of the
+ * reference's Python API is {TRANSIENT, SHIFT_X0, FEATURES, SHIFT_X0}). */
+enum clode_op { CLODE_OP_TRANSIENT = 0, CLODE_OP_FEATURES = 1, CLODE_OP_TRAJECTORY = 2, CLODE_OP_SHIFT_X0 = 3 };
+int clode_sim_chain(clode_sim *sim, const int *ops, int n_ops, int use_graph);
+/* Autotuner: times the persistent kernel of this simulator's kind on members
+ * [0, sample) (sample <= 0: all) for register caps {none, 128, 96, 80, 64} and
+ * block sizes {64, 128}, keeps the fastest ("maxrregcount", "block_size",
+ * schedule 1) and returns its time.  The sampled members' dt and RNG state are
+ * restored; the observer is re-initialised at the next features run. */
+int clode_sim_autotune(clode_sim *sim, long long sample, double *best_ms);
 /* Number of kernel launches this library has issued since it was loaded
  * (ensemble kernels and the conversion/seeding kernels alike). */
 unsigned long long clode_launch_count(void);
@@ -271,6 +284,34 @@ int clode_sim_features_noalloc(clode_sim *sim, long long n_pts, const void *x0, 
 /* Register-file footprint of the built kernels: registers per thread of the features
  * (or transient / trajectory) kernel, as reported by the driver. */
 int clode_sim_kernel_info(clode_sim *sim, const char *kernel, int *registers, int *max_threads);
+
+/* ------------------------------------- learned surrogate (no reference counterpart) */
+/* An MLP 2 -> 256 -> 256 -> 256 -> n_heads x n_outputs (ReLU hidden layers),
+ * BF16 tensor-core layers with FP32 accumulation, trained on the device.  It
+ * learns a feature map from engine-computed points and screens large grids.
+ * Inputs x are [n x 2] float rows, targets / predictions [n x n_outputs].
+ * n_heads * n_outputs must be 16, 32 or 64. */
+typedef struct clode_mlp clode_mlp;
+int clode_mlp_create(int n_outputs, int n_heads, int device, unsigned long long seed, clode_mlp **out);
+int clode_mlp_destroy(clode_mlp *net);
+int clode_mlp_param_count(clode_mlp *net, size_t *n);
+/* parameters, float32: W1 [2x256], b1, W2 [256x256], b2, W3 [256x256], b3, Wh [256 x H*K], bh */
+int clode_mlp_get_params(clode_mlp *net, float *out, size_t n);
+int clode_mlp_set_params(clode_mlp *net, const float *in, size_t n);
+/* loss and gradient vector of one batch (every head fits the same targets); no update */
+int clode_mlp_gradients(clode_mlp *net, const float *x, const float *y, int n, float *grads, size_t n_grads,
+                        float *loss);
+/* Adam on mean-square error, `steps` minibatches of `batch` rows of a shuffled copy of
+ * (x, y); loss_history (steps floats) may be NULL.  Steps after the first replay a CUDA graph. */
+int clode_mlp_train(clode_mlp *net, const float *x, const float *y, long long n, int steps, int batch, float lr,
+                    unsigned long long seed, float *loss_history);
+/* mean and standard deviation over the heads, [n x n_outputs] each; heads [n x H*K] may be NULL */
+int clode_mlp_predict(clode_mlp *net, const float *x, long long n, float *mean, float *spread, float *heads);
+/* flags of the last prediction laid out as an nx x ny grid (point iy*nx + ix):
+ * bit 0 = head spread above spread_thr[k], bit 1 = jump to a 4-neighbour above jump_thr[k] */
+int clode_mlp_screen(clode_mlp *net, int nx, int ny, const float *spread_thr, const float *jump_thr, int *flags);
+/* wall time of the last train and predict calls, milliseconds */
+int clode_mlp_timings(clode_mlp *net, double *train_ms, double *predict_ms);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,81 @@
+"""The surrogate network's own tensor-core kernels against the NumPy oracle
+(forward and gradients), its training, its screening, and what it gains over
+integrating every point of a feature map with the plain engine."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as MO
+
+pytestmark = pytest.mark.gpu
+
+
+def _net(K=4, H=4, seed=3):
+    from clode_gb300.surrogate import MLP
+    return MLP(K, H, 0, seed)
+
+
+def test_tensor_core_forward_matches_oracle():
+    net = _net()
+    p = net.get_params()
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, (1000, 2)).astype(np.float32)  # not a multiple of the 128-row tile
+    mean, spread, heads = net.predict(x, heads=True)
+    ref = MO.forward(p, x, 16)["out"]
+    scale = np.abs(ref).max()
+    # tolerance: BF16 activations; a value on a rounding tie may round the other way
+    # when the GPU accumulates in FP32 and the oracle in float64
+    np.testing.assert_allclose(heads, ref, rtol=2e-2, atol=2e-2 * scale)
+    r4 = ref.reshape(-1, 4, 4)
+    np.testing.assert_allclose(mean, r4.mean(axis=1), rtol=2e-2, atol=2e-2 * scale)
+
+
+def test_gradients_match_oracle():
+    net = _net(seed=5)
+    p = net.get_params()
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, (777, 2)).astype(np.float32)
+    y = np.stack([np.sin(3 * x[:, 0]), np.cos(2 * x[:, 1]), x[:, 0] * x[:, 1], x[:, 0] ** 2], axis=1)
+    y = y.astype(np.float32)
+    loss, g = net.gradients(x, y)
+    lref, gref, _ = MO.loss_and_gradients(p, x, y, 4, 4)
+    assert abs(loss - lref) <= 1e-3 * abs(lref) + 1e-6
+    parts = MO.split(g, 16)
+    refs = MO.split(gref, 16)
+    for name in parts:
+        a, b = parts[name].ravel(), refs[name].ravel()
+        err = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30)
+        # tolerance: BF16 rounding of activations and back-propagated gradients
+        assert err < 2e-2, (name, err)
+
+
+def test_training_fits_a_smooth_map():
+    net = _net(seed=7)
+    rng = np.random.default_rng(2)
+    x = rng.uniform(-1, 1, (65536, 2)).astype(np.float32)
+    y = np.stack([np.sin(3 * x[:, 0]) * np.cos(2 * x[:, 1]), x[:, 0] * x[:, 1], np.exp(-x[:, 0] ** 2),
+                  x[:, 1] ** 3], axis=1).astype(np.float32)
+    hist = net.train(x, y, steps=1500, batch=2048, lr=2e-3)
+    assert np.isfinite(hist).all()
+    assert hist[-50:].mean() < 0.02 * hist[:5].mean()
+    xt = rng.uniform(-1, 1, (4096, 2)).astype(np.float32)
+    yt = np.stack([np.sin(3 * xt[:, 0]) * np.cos(2 * xt[:, 1]), xt[:, 0] * xt[:, 1], np.exp(-xt[:, 0] ** 2),
+                   xt[:, 1] ** 3], axis=1)
+    mean, spread = net.predict(xt)
+    assert np.sqrt(np.mean((mean - yt) ** 2)) < 0.05
+
+
+def test_screen_flags_the_discontinuity():
+    net = _net(seed=9)
+    rng = np.random.default_rng(4)
+    x = rng.uniform(-1, 1, (65536, 2)).astype(np.float32)
+    y = np.repeat((x[:, :1] > 0).astype(np.float32), 4, axis=1)  # a step along x0 = 0
+    net.train(x, y, steps=800, batch=2048, lr=2e-3)
+    n = 64
+    g = np.linspace(-1, 1, n)
+    G0, G1 = np.meshgrid(g, g, indexing="xy")
+    net.predict(np.stack([G0.ravel(), G1.ravel()], axis=1))
+    flags = net.screen(n, n, np.full(4, 10.0), np.full(4, 0.25)).reshape(n, n)
+    cols = np.nonzero(flags.any(axis=0))[0]
+    assert cols.size > 0
+    assert np.abs(g[cols]).max() < 0.2  # only next to the step
+    assert flags[:, :20].sum() == 0 and flags[:, -20:].sum() == 0
