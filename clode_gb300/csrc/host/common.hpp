@@ -42,6 +42,7 @@ struct ProgramSpec {
     bool prec_div = true;               // IEEE division; false: approximate (2 ulp)
     bool ftz = false;                   // flush FP32 denormals to zero
     int maxrregcount = 0;               // 0: no register cap
+    bool fast_math = false;             // --use_fast_math: approximate exp/log/pow/sin/cos/sqrt (+ ftz, fast division)
     std::string arch;                   // e.g. "sm_103a"
 };
 

@@ -1,24 +1,27 @@
 // Kernels of the learned surrogate: a multilayer perceptron
-//   x (2) -> 256 -> 256 -> 256 -> H heads x K outputs,  ReLU hidden layers,
+//   x (2) -> 256 (sine) -> 256 (ReLU) -> 256 (ReLU) -> H heads x K outputs,
 // trained on feature maps computed by the ensemble engine, used to screen
-// large parameter grids.
+// large parameter grids.  The sine first layer (a learned Fourier
+// encoding of the two parameters) lets the network resolve the sharp but
+// smooth ridges of a feature map that a ReLU first layer blurs.
 //
 // The 256-wide layers and the heads run on the 5th-generation tensor cores:
 // tcgen05.mma (kind::f16, BF16 operands, FP32 accumulation in tensor memory),
 // one 128-row tile of activations per MMA group, the layer's weights resident
 // in shared memory for the whole persistent CTA, the accumulator read back
-// with tcgen05.ld for a fused epilogue (bias + ReLU, or the ReLU-derivative
-// mask in the backward pass).  Operand tiles are written to shared memory in
-// the canonical K-major, non-swizzled core-matrix layout (8 rows x 16 bytes
-// per core matrix; LBO = 128 B between core matrices along K, SBO = K * 16 B
-// between 8-row groups) that the shared-memory matrix descriptors describe.
-// Weight-gradient reductions over the batch (X^T dZ), the 2-wide input layer,
-// the loss and Adam are small and run on the CUDA cores.
+// with tcgen05.ld for a fused epilogue (bias + ReLU, or the derivative of the
+// activation in the backward pass).  All BF16 operands live in global memory
+// in core-matrix order (mlp.hpp), so the weights and each 128-row activation
+// tile arrive in shared memory by one bulk asynchronous copy each
+// (cp.async.bulk, completion on an mbarrier), and the next tile's copy is
+// issued as soon as the MMA group has consumed the current one.  Weight
+// gradients (X^T dZ over the batch), the 2-wide input layer, the loss and
+// Adam are small and run on the CUDA cores.
 //
 // Every wait on an mbarrier is bounded: one thread polls with an iteration
 // limit, publishes the outcome through shared memory, and on a timeout the
-// CTA records an error flag, skips its remaining tiles, frees its tensor
-// memory and returns.
+// CTA records an error flag, skips its remaining tiles, gives the operation
+// in flight a second bounded wait, frees its tensor memory and returns.
 #include "common.hpp"
 #include "mlp.hpp"
 
@@ -26,8 +29,6 @@
 
 namespace clode {
 namespace mlp {
-
-typedef __nv_bfloat16 bf16;
 
 // ------------------------------------------------------------------ PTX --
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -50,6 +51,39 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity)
     return ok != 0u;
 }
 
+constexpr long kSpinLimit = 1L << 26;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+{
+    for (long it = 0; it < kSpinLimit; ++it)
+        if (mbar_test(bar, parity))
+            return true;
+    return false;
+}
+
+// arrive on the barrier and expect `bytes` of asynchronous copies in this phase
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    constexpr uint32_t kChunk = 32768;
+    const char *s = (const char *)src;
+    char *d = (char *)dst;
+    for (uint32_t off = 0; off < bytes; off += kChunk) {
+        uint32_t n = bytes - off < kChunk ? bytes - off : kChunk;
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(d + off)),
+            "l"(__cvta_generic_to_global(s + off)), "r"(n), "r"(smem_u32(bar))
+            : "memory");
+    }
+}
+
 __device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols)
 {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
@@ -65,7 +99,6 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, M x N x 16, BF16 in, FP32 accumulate
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
@@ -119,22 +152,14 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// byte offset of element (r, k) of a K-wide K-major tile in core-matrix layout
-__device__ __forceinline__ uint32_t cm_offset(int r, int k, int K)
-{
-    return (uint32_t)((r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
-}
-
 // ------------------------------------------------------- tensor-core layer --
 // Y[m, n] = epilogue( sum_k X[m, k] * B[n, k] + bias[n] ),  m < M, n < N
-//   X: BF16 [M x K] row-major, B: BF16 [N x K] row-major (K-major operand)
-//   EPI_RELU_BF16:  Y = max(. + bias, 0)  -> BF16 [M x N]
-//   EPI_BIAS_F32:   Y = . + bias          -> FP32 [M x N]
-//   EPI_MASK_BF16:  Y = . * (mask[m, n] > 0) -> BF16 [M x N]  (no bias)
-enum { EPI_RELU_BF16 = 0, EPI_BIAS_F32 = 1, EPI_MASK_BF16 = 2 };
-
-constexpr int kTileM = 128;
-constexpr long kSpinLimit = 1L << 26;
+//   X: BF16 [M x K] core-matrix order (whole 128-row tiles), B: BF16 [N x K] core-matrix order
+//   EPI_RELU_BF16:  Y = max(. + bias, 0)        -> BF16 [M x N] core-matrix order
+//   EPI_BIAS_F32:   Y = . + bias                -> FP32 [M x N] row-major
+//   EPI_MASK_BF16:  Y = . * (mask[m, n] > 0)    -> BF16 core-matrix order (no bias)
+//   EPI_MUL_BF16:   Y = . * mask[m, n]          -> BF16 core-matrix order (no bias)
+enum { EPI_RELU_BF16 = 0, EPI_BIAS_F32 = 1, EPI_MASK_BF16 = 2, EPI_MUL_BF16 = 3 };
 
 template <int K, int N, int EPI>
 __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X, int M, const bf16 *__restrict__ B,
@@ -144,60 +169,71 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
 {
     static_assert(K % 16 == 0 && N % 16 == 0 && N >= 16 && N <= 256, "tile shape");
     constexpr uint32_t kCols = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    constexpr uint32_t kABytes = kTileM * K * 2, kBBytes = N * K * 2;
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sA = smem;                         // kTileM x K bf16
-    unsigned char *sB = smem + kTileM * K * 2;        // N x K bf16
-    uint64_t *bar = (uint64_t *)(sB + N * K * 2);
-    uint32_t *tslot = (uint32_t *)(bar + 1);
+    unsigned char *sA = smem;             // kTileM x K bf16, core-matrix order
+    unsigned char *sB = smem + kABytes;   // N x K bf16, core-matrix order
+    uint64_t *bar_ld = (uint64_t *)(sB + kBBytes);
+    uint64_t *bar_mma = bar_ld + 1;
+    uint32_t *tslot = (uint32_t *)(bar_mma + 1);
     volatile int *sflag = (volatile int *)(tslot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tiles = (M + kTileM - 1) / kTileM;
+    int tile = blockIdx.x;
     if (warp == 0)
         tmem_alloc(tslot, kCols);
     if (tid == 0) {
-        mbar_init(bar, 1);
+        mbar_init(bar_ld, 1);
+        mbar_init(bar_mma, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *sflag = 0;
-    }
-    // weights: resident for the whole CTA
-    for (int idx = tid; idx < N * (K / 8); idx += blockDim.x) {
-        int r = idx / (K / 8), c = idx % (K / 8);
-        uint4 v = *(const uint4 *)(B + (size_t)r * K + c * 8);
-        *(uint4 *)(sB + cm_offset(r, c * 8, K)) = v;
+        if (tile < tiles) {  // the weights and the first tile arrive on the first phase
+            mbar_expect_tx(bar_ld, kBBytes + kABytes);
+            bulk_g2s(sB, B, kBBytes, bar_ld);
+            bulk_g2s(sA, X + (size_t)tile * kTileM * K, kABytes, bar_ld);
+        }
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
     const uint32_t idesc = idesc_bf16(kTileM, N);
-    uint32_t parity = 0;
+    uint32_t ph_ld = 0, ph_mma = 0;
+    int pending = 0;  // thread 0: 1 = a copy may be in flight, 2 = an MMA group may be in flight
     bool failed = false;
 
-    for (int tile = blockIdx.x; tile * kTileM < M && !failed; tile += gridDim.x) {
+    for (; tile < tiles; tile += gridDim.x) {
         const int row0 = tile * kTileM;
-        for (int idx = tid; idx < kTileM * (K / 8); idx += blockDim.x) {
-            int r = idx / (K / 8), c = idx % (K / 8);
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (row0 + r < M)
-                v = *(const uint4 *)(X + (size_t)(row0 + r) * K + c * 8);
-            *(uint4 *)(sA + cm_offset(r, c * 8, K)) = v;
-        }
-        fence_async_smem();  // generic-proxy stores -> visible to the tensor core
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
         if (tid == 0) {
-            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+            int st = 0;
+            if (!mbar_wait_bounded(bar_ld, ph_ld)) {
+                st = 1;
+                pending = 1;
+            } else {
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
 #pragma unroll
-            for (int s = 0; s < K / 16; ++s)
-                mma_bf16(tmem, smem_desc(a0 + s * 256, 128, K * 16), smem_desc(b0 + s * 256, 128, K * 16), idesc,
-                         s > 0 ? 1u : 0u);
-            mma_commit(bar);
-            bool done = false;
-            for (long it = 0; it < kSpinLimit && !done; ++it)
-                done = mbar_test(bar, parity);
-            *sflag = done ? 0 : 1;
+                for (int s = 0; s < K / 16; ++s)
+                    mma_bf16(tmem, smem_desc(a0 + s * 256, 128, K * 16), smem_desc(b0 + s * 256, 128, K * 16), idesc,
+                             s > 0 ? 1u : 0u);
+                mma_commit(bar_mma);
+                if (!mbar_wait_bounded(bar_mma, ph_mma)) {
+                    st = 2;
+                    pending = 2;
+                } else {
+                    // the MMA group has consumed sA: fetch the next tile behind the epilogue
+                    const int next = tile + gridDim.x;
+                    if (next < tiles) {
+                        mbar_expect_tx(bar_ld, kABytes);
+                        bulk_g2s(sA, X + (size_t)next * kTileM * K, kABytes, bar_ld);
+                    }
+                }
+            }
+            *sflag = st;
         }
+        ph_ld ^= 1u;
+        ph_mma ^= 1u;
         __syncthreads();
         if (*sflag) {
             failed = true;
@@ -205,7 +241,6 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
                 atomicExch(err, 1);
             break;
         }
-        parity ^= 1u;
         tc_fence_after();
         const int m = row0 + warp * 32 + lane;
         const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
@@ -223,20 +258,25 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
                         *(float4 *)(y + k) = o;
                     }
                 } else {
+                    const size_t o0 = tiled_offset(m, c0, N), o1 = tiled_offset(m, c0 + 8, N);
                     __align__(16) bf16 o[16];
                     if (EPI == EPI_RELU_BF16) {
 #pragma unroll
                         for (int k = 0; k < 16; ++k)
                             o[k] = __float2bfloat16_rn(fmaxf(v[k] + bias[c0 + k], 0.0f));
                     } else {
-                        const bf16 *mk = mask + (size_t)m * N + c0;
+                        __align__(16) bf16 mk[16];
+                        *(uint4 *)&mk[0] = *(const uint4 *)(mask + o0);
+                        *(uint4 *)&mk[8] = *(const uint4 *)(mask + o1);
 #pragma unroll
-                        for (int k = 0; k < 16; ++k)
-                            o[k] = __float2bfloat16_rn(__bfloat162float(mk[k]) > 0.0f ? v[k] : 0.0f);
+                        for (int k = 0; k < 16; ++k) {
+                            float g = __bfloat162float(mk[k]);
+                            o[k] = __float2bfloat16_rn(EPI == EPI_MUL_BF16 ? v[k] * g : (g > 0.0f ? v[k] : 0.0f));
+                        }
                     }
-                    bf16 *y = (bf16 *)Y + (size_t)m * N + c0;
-                    *(uint4 *)y = *(const uint4 *)&o[0];
-                    *(uint4 *)(y + 8) = *(const uint4 *)&o[8];
+                    bf16 *y = (bf16 *)Y;
+                    *(uint4 *)(y + o0) = *(const uint4 *)&o[0];
+                    *(uint4 *)(y + o1) = *(const uint4 *)&o[8];
                 }
             }
         }
@@ -245,11 +285,12 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
         tc_fence_after();
     }
     if (failed && tid == 0) {
-        // the MMA group never signalled: give it one more bounded chance to
-        // finish before its tensor memory is released
-        for (long it = 0; it < kSpinLimit; ++it)
-            if (mbar_test(bar, parity))
-                break;
+        // the copy or MMA group never signalled: one more bounded chance to
+        // finish before the shared and tensor memory are released
+        if (pending == 1)
+            mbar_wait_bounded(bar_ld, ph_ld ^ 1u);
+        else if (pending == 2)
+            mbar_wait_bounded(bar_mma, ph_mma ^ 1u);
     }
     tc_fence_before();
     __syncthreads();
@@ -280,116 +321,259 @@ void launch_linear(const bf16 *X, int M, const bf16 *B, const float *bias, const
 }
 
 // ---------------------------------------------------------- CUDA-core parts --
-// input layer: h1 = relu(x W1 + b1), x FP32 [M x 2], W1 FP32 [2 x 256]
-__global__ void k_input_layer(const float *__restrict__ x, int M, const float *__restrict__ W1,
-                              const float *__restrict__ b1, bf16 *__restrict__ h1)
+// thread index -> (row m, 8-column chunk c8) of a W-wide core-matrix-order
+// matrix such that a warp writes contiguous 16-byte pieces
+__device__ __forceinline__ void chunk_coords(size_t idx, int W, long long &m, int &c8)
 {
-    size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    size_t total = (size_t)M * kWidth;
-    for (; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
-        size_t m = idx / kWidth;
-        int n = (int)(idx % kWidth);
-        float z = x[2 * m] * W1[n] + x[2 * m + 1] * W1[kWidth + n] + b1[n];
-        h1[idx] = __float2bfloat16_rn(fmaxf(z, 0.0f));
+    const int chunks = W / 8;
+    long long grp = (long long)(idx / (size_t)(chunks * 8));
+    int rem = (int)(idx % (size_t)(chunks * 8));
+    c8 = rem / 8;
+    m = grp * 8 + (rem & 7);
+}
+
+// input layer: z = x W1 + b1 (x FP32 [M x 2], W1 FP32 [2 x 256]);
+// h1 = sin z, c1 = cos z (BF16, core-matrix order)
+__global__ void k_input_layer(const float *__restrict__ x, int M, const float *__restrict__ W1,
+                              const float *__restrict__ b1, bf16 *__restrict__ h1, bf16 *__restrict__ c1)
+{
+    const size_t total = (size_t)tiled_rows(M) * (kWidth / 8);
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        long long m;
+        int c8;
+        chunk_coords(idx, kWidth, m, c8);
+        if (m >= M)
+            continue;
+        const float x0 = x[2 * m], x1 = x[2 * m + 1];
+        __align__(16) bf16 hs[8], hc[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int n = c8 * 8 + j;
+            const float z = x0 * W1[n] + x1 * W1[kWidth + n] + b1[n];
+            float sz, cz;
+            sincosf(z, &sz, &cz);
+            hs[j] = __float2bfloat16_rn(sz);
+            hc[j] = __float2bfloat16_rn(cz);
+        }
+        const size_t o = tiled_offset(m, c8 * 8, kWidth);
+        *(uint4 *)(h1 + o) = *(const uint4 *)hs;
+        *(uint4 *)(c1 + o) = *(const uint4 *)hc;
     }
 }
 
-// loss: heads predict the same K targets; out FP32 [M x H*K], y FP32 [M x K]
-// dz = 2 (out - y) / (M * H * K) as BF16, loss accumulates the mean square error
+// loss: heads predict the same K targets; out FP32 [M x H*K] row-major, y FP32 [M x K];
+// dz = 2 (out - y) / (M * H * K) as BF16 (core-matrix order, width H*K);
+// loss accumulates the mean square error
 __global__ void k_mse(const float *__restrict__ out, const float *__restrict__ y, int M, int H, int K,
                       bf16 *__restrict__ dz, float *__restrict__ loss)
 {
     const int HK = H * K;
-    size_t total = (size_t)M * HK;
+    const size_t total = (size_t)tiled_rows(M) * (HK / 8);
+    const float scale = 2.0f / ((float)M * (float)HK);
     float local = 0.0f;
-    const float scale = 2.0f / (float)total;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
          idx += (size_t)gridDim.x * blockDim.x) {
-        size_t m = idx / HK;
-        int k = (int)(idx % HK) % K;
-        float d = out[idx] - y[m * K + k];
-        local += d * d;
-        dz[idx] = __float2bfloat16_rn(scale * d);
+        long long m;
+        int c8;
+        chunk_coords(idx, HK, m, c8);
+        if (m >= M)
+            continue;
+        __align__(16) bf16 o[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int c = c8 * 8 + j;
+            const float d = out[(size_t)m * HK + c] - y[(size_t)m * K + c % K];
+            local += d * d;
+            o[j] = __float2bfloat16_rn(scale * d);
+        }
+        *(uint4 *)(dz + tiled_offset(m, c8 * 8, HK)) = *(const uint4 *)o;
     }
     for (int off = 16; off > 0; off >>= 1)
         local += __shfl_down_sync(0xffffffffu, local, off);
     if ((threadIdx.x & 31) == 0)
-        atomicAdd(loss, local / (float)total);
+        atomicAdd(loss, local / ((float)M * (float)HK));
 }
 
-__device__ __forceinline__ float to_f(float v) { return v; }
-__device__ __forceinline__ float to_f(bf16 v) { return __bfloat162float(v); }
-
-// weight gradient: G[k, n] = sum_m A[m, k] * D[m, n]  (A BF16 or FP32 [M x Kd], D BF16 [M x N]),
-// bias gradient g[n] = sum_m D[m, n];  one 16 x 16 output tile per block
-template <typename TA>
-__global__ void k_weight_grad(const TA *__restrict__ A, int Kd, const bf16 *__restrict__ D, int N, int M,
-                              float *__restrict__ G, float *__restrict__ g)
+// weight gradient over one chunk of batch rows:
+//   G[k, n] += sum_m A[m, k] D[m, n],  g[n] += sum_m D[m, n]  (g from the k0 = 0 blocks)
+// A: BF16 [M x Kd], D: BF16 [M x N], both core-matrix order.  A block owns a
+// 64 x TN output tile and rows [z * rows_per_block, ...); 256 threads, each
+// 4 x (TN / 16) outputs.
+template <int TN>
+__global__ void __launch_bounds__(256) k_weight_grad(const bf16 *__restrict__ A, int Kd, const bf16 *__restrict__ D,
+                                                     int N, int M, int rows_per_block, float *__restrict__ G,
+                                                     float *__restrict__ g)
 {
-    __shared__ float sa[64][17];
-    __shared__ float sd[64][17];
-    const int k0 = blockIdx.x * 16, n0 = blockIdx.y * 16;
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 256 threads: (k, n) = (ty, tx)
-    float acc = 0.0f, bacc = 0.0f;
-    for (int m0 = 0; m0 < M; m0 += 64) {
-        for (int i = threadIdx.x; i < 64 * 16; i += 256) {
-            int mm = i / 16, c = i % 16;
-            int m = m0 + mm;
-            float av = 0.0f, dv = 0.0f;
-            if (m < M) {
-                if (k0 + c < Kd)
-                    av = to_f(A[(size_t)m * Kd + k0 + c]);
-                if (n0 + c < N)
-                    dv = __bfloat162float(D[(size_t)m * N + n0 + c]);
-            }
-            sa[mm][c] = av;
-            sd[mm][c] = dv;
+    constexpr int TK = 64, RM = 32, RN = TN / 16;
+    __shared__ __align__(16) float sa[RM][TK];
+    __shared__ __align__(16) float sd[RM][TN];
+    const int k0 = blockIdx.x * TK, n0 = blockIdx.y * TN;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int m_begin = blockIdx.z * rows_per_block;
+    const int m_end = min(M, m_begin + rows_per_block);
+    float acc[4][RN];
+    float bacc[RN];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < RN; ++j)
+            acc[i][j] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < RN; ++j)
+        bacc[j] = 0.0f;
+    for (int m0 = m_begin; m0 < m_end; m0 += RM) {
+        // stage RM rows: A columns [k0, k0+64) and D columns [n0, n0+TN), 8 values per load
+        for (int i = tid; i < RM * (TK / 8); i += 256) {
+            const int mm = i / (TK / 8), c8 = i % (TK / 8);
+            const int m = m0 + mm;
+            __align__(16) bf16 v[8];
+            if (m < m_end && k0 + c8 * 8 < Kd)
+                *(uint4 *)v = *(const uint4 *)(A + tiled_offset(m, k0 + c8 * 8, Kd));
+            else
+                *(uint4 *)v = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                sa[mm][c8 * 8 + j] = __bfloat162float(v[j]);
+        }
+        for (int i = tid; i < RM * (TN / 8); i += 256) {
+            const int mm = i / (TN / 8), c8 = i % (TN / 8);
+            const int m = m0 + mm;
+            __align__(16) bf16 v[8];
+            if (m < m_end && n0 + c8 * 8 < N)
+                *(uint4 *)v = *(const uint4 *)(D + tiled_offset(m, n0 + c8 * 8, N));
+            else
+                *(uint4 *)v = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                sd[mm][c8 * 8 + j] = __bfloat162float(v[j]);
         }
         __syncthreads();
 #pragma unroll 8
-        for (int mm = 0; mm < 64; ++mm) {
-            acc += sa[mm][ty] * sd[mm][tx];
-            bacc += sd[mm][tx];
+        for (int mm = 0; mm < RM; ++mm) {
+            const float4 a = *(const float4 *)&sa[mm][ty * 4];
+            float d[RN];
+#pragma unroll
+            for (int j = 0; j < RN; ++j)
+                d[j] = sd[mm][tx * RN + j];
+#pragma unroll
+            for (int j = 0; j < RN; ++j) {
+                acc[0][j] += a.x * d[j];
+                acc[1][j] += a.y * d[j];
+                acc[2][j] += a.z * d[j];
+                acc[3][j] += a.w * d[j];
+                bacc[j] += d[j];
+            }
         }
         __syncthreads();
     }
-    if (k0 + ty < Kd && n0 + tx < N)
-        G[(size_t)(k0 + ty) * N + n0 + tx] = acc;
-    if (g && blockIdx.x == 0 && ty == 0 && n0 + tx < N)
-        g[n0 + tx] = bacc;
-}
-
-// Adam on FP32 master weights; refreshes the BF16 copies the tensor cores read:
-// wt[n, k] = w[k, n] (forward operand) and wk[k, n] = w[k, n] (backward operand)
-__global__ void k_adam(float *__restrict__ w, const float *__restrict__ grad, float *__restrict__ m1,
-                       float *__restrict__ m2, int rows, int cols, float lr, float b1, float b2, float eps,
-                       const int *__restrict__ step, bf16 *__restrict__ wt, bf16 *__restrict__ wk)
-{
-    const int t = *step;
-    const float c1 = 1.0f - powf(b1, (float)t), c2 = 1.0f - powf(b2, (float)t);
-    size_t total = (size_t)rows * cols;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (size_t)gridDim.x * blockDim.x) {
-        float gr = grad[idx];
-        float a = b1 * m1[idx] + (1.0f - b1) * gr;
-        float b = b2 * m2[idx] + (1.0f - b2) * gr * gr;
-        m1[idx] = a;
-        m2[idx] = b;
-        float v = w[idx] - lr * (a / c1) / (sqrtf(b / c2) + eps);
-        w[idx] = v;
-        int r = (int)(idx / cols), c = (int)(idx % cols);
-        if (wt)
-            wt[(size_t)c * rows + r] = __float2bfloat16_rn(v);
-        if (wk)
-            wk[idx] = __float2bfloat16_rn(v);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int k = k0 + ty * 4 + i;
+        if (k >= Kd)
+            continue;
+#pragma unroll
+        for (int j = 0; j < RN; ++j) {
+            const int n = n0 + tx * RN + j;
+            if (n < N)
+                atomicAdd(&G[(size_t)k * N + n], acc[i][j]);
+        }
+    }
+    if (g && blockIdx.x == 0 && ty == 0) {
+#pragma unroll
+        for (int j = 0; j < RN; ++j) {
+            const int n = n0 + tx * RN + j;
+            if (n < N)
+                atomicAdd(&g[n], bacc[j]);
+        }
     }
 }
 
-__global__ void k_step_increment(int *step) { *step += 1; }
+// input-layer gradient: G1[k, n] += sum_m x[m, k] D[m, n] (k < 2), g1[n] += sum_m D[m, n];
+// one thread per column n, rows [blockIdx.x * rows_per_block, ...)
+__global__ void __launch_bounds__(256) k_weight_grad_input(const float *__restrict__ x, const bf16 *__restrict__ D,
+                                                           int M, int rows_per_block, float *__restrict__ G,
+                                                           float *__restrict__ g)
+{
+    const int n = threadIdx.x;
+    const int m_begin = blockIdx.x * rows_per_block;
+    const int m_end = min(M, m_begin + rows_per_block);
+    float a0 = 0.0f, a1 = 0.0f, ab = 0.0f;
+#pragma unroll 8
+    for (int m = m_begin; m < m_end; ++m) {
+        const float d = __bfloat162float(D[tiled_offset(m, n, kWidth)]);
+        a0 += x[2 * m] * d;
+        a1 += x[2 * m + 1] * d;
+        ab += d;
+    }
+    atomicAdd(&G[n], a0);
+    atomicAdd(&G[kWidth + n], a1);
+    atomicAdd(&g[n], ab);
+}
 
-// rows [cursor*B, cursor*B + B) of the epoch's shuffled data into the batch buffers
+// BF16 operand images of the tensor-core weights from the FP32 masters
+struct ImageSet {
+    WeightImages im[3];
+    int n;
+};
+
+__device__ __forceinline__ void store_images(const ImageSet &set, size_t idx, float v)
+{
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        if (q >= set.n)
+            break;
+        const WeightImages &w = set.im[q];
+        const size_t size = (size_t)w.k_in * w.n_out;
+        if (idx >= w.offset && idx < w.offset + size) {
+            const int r = (int)((idx - w.offset) / w.n_out), c = (int)((idx - w.offset) % w.n_out);
+            const bf16 b = __float2bfloat16_rn(v);
+            w.fwd[tiled_offset(c, r, w.k_in)] = b;
+            w.bwd[tiled_offset(r, c, w.n_out)] = b;
+        }
+    }
+}
+
+// Adam over the whole parameter vector; refreshes the BF16 images; thread 0
+// also advances the batch cursor and appends the step's loss to the history
+__global__ void k_adam_all(float *__restrict__ w, const float *__restrict__ grad, float *__restrict__ m1,
+                           float *__restrict__ m2, size_t n, float lr, float b1, float b2, float eps,
+                           const int *__restrict__ step, ImageSet set, int *__restrict__ cursor,
+                           const float *__restrict__ loss, float *__restrict__ loss_hist, int *__restrict__ hist_index)
+{
+    const int t = *step;
+    const float c1 = 1.0f - powf(b1, (float)t), c2 = 1.0f - powf(b2, (float)t);
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const float gr = grad[idx];
+        const float a = b1 * m1[idx] + (1.0f - b1) * gr;
+        const float b = b2 * m2[idx] + (1.0f - b2) * gr * gr;
+        m1[idx] = a;
+        m2[idx] = b;
+        const float v = w[idx] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+        w[idx] = v;
+        store_images(set, idx, v);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (cursor)
+            *cursor += 1;
+        if (loss_hist && hist_index) {
+            loss_hist[*hist_index] = *loss;
+            *hist_index += 1;
+        }
+    }
+}
+
+__global__ void k_write_images(const float *__restrict__ w, ImageSet set, size_t n)
+{
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x)
+        store_images(set, idx, w[idx]);
+}
+
+// rows [cursor*B, cursor*B + B) of the epoch's shuffled data into the batch
+// buffers; thread 0 also advances the step counter and clears the loss
 __global__ void k_gather_batch(const float *__restrict__ xs, const float *__restrict__ ys, int n_rows, int K,
-                               int B, int *__restrict__ cursor, float *__restrict__ xb, float *__restrict__ yb)
+                               int B, const int *__restrict__ cursor, float *__restrict__ xb, float *__restrict__ yb,
+                               int *__restrict__ step, float *__restrict__ loss)
 {
     const int c = *cursor;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B; i += gridDim.x * blockDim.x) {
@@ -399,9 +583,11 @@ __global__ void k_gather_batch(const float *__restrict__ xs, const float *__rest
         for (int k = 0; k < K; ++k)
             yb[(size_t)i * K + k] = ys[(size_t)r * K + k];
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *step += 1;
+        *loss = 0.0f;
+    }
 }
-
-__global__ void k_cursor_increment(int *cursor) { *cursor += 1; }
 
 // head statistics: mean and standard deviation over the H heads
 __global__ void k_head_stats(const float *__restrict__ out, long long M, int H, int K, float *__restrict__ mean,
@@ -466,96 +652,130 @@ void after_launch(const char *what)
     count_launch();
     check_cuda(cudaGetLastError(), what);
 }
+ImageSet image_set(const WeightImages *img, int n)
+{
+    if (n < 0 || n > 3)
+        fail(CLODE_ERR_INTERNAL, "at most 3 weight images");
+    ImageSet s{};
+    for (int i = 0; i < n; ++i)
+        s.im[i] = img[i];
+    s.n = n;
+    return s;
+}
 }  // namespace
 
-void linear_relu(const bf16 *X, int M, const bf16 *Wt, const float *b, bf16 *Y, int *err, int sms, cudaStream_t s)
+void linear_relu(const bf16 *X, int M, const bf16 *Wfwd, const float *b, bf16 *Y, int *err, int sms, cudaStream_t s)
 {
-    launch_linear<kWidth, kWidth, EPI_RELU_BF16>(X, M, Wt, b, nullptr, Y, err, sms, s);
+    launch_linear<kWidth, kWidth, EPI_RELU_BF16>(X, M, Wfwd, b, nullptr, Y, err, sms, s);
 }
 
-void linear_heads(const bf16 *X, int M, const bf16 *Wt, const float *b, float *Y, int n_out, int *err, int sms,
+void linear_heads(const bf16 *X, int M, const bf16 *Wfwd, const float *b, float *Y, int n_out, int *err, int sms,
                   cudaStream_t s)
 {
     if (n_out == 16)
-        launch_linear<kWidth, 16, EPI_BIAS_F32>(X, M, Wt, b, nullptr, Y, err, sms, s);
+        launch_linear<kWidth, 16, EPI_BIAS_F32>(X, M, Wfwd, b, nullptr, Y, err, sms, s);
     else if (n_out == 32)
-        launch_linear<kWidth, 32, EPI_BIAS_F32>(X, M, Wt, b, nullptr, Y, err, sms, s);
+        launch_linear<kWidth, 32, EPI_BIAS_F32>(X, M, Wfwd, b, nullptr, Y, err, sms, s);
     else if (n_out == 64)
-        launch_linear<kWidth, 64, EPI_BIAS_F32>(X, M, Wt, b, nullptr, Y, err, sms, s);
+        launch_linear<kWidth, 64, EPI_BIAS_F32>(X, M, Wfwd, b, nullptr, Y, err, sms, s);
     else
         fail(CLODE_ERR_INVALID_ARGUMENT, "heads x outputs must be 16, 32 or 64 (got %d)", n_out);
 }
 
-void linear_back_hidden(const bf16 *dZ, int M, const bf16 *Wk, const bf16 *mask, bf16 *dX, int *err, int sms,
-                        cudaStream_t s)
+void linear_back_relu(const bf16 *dZ, int M, const bf16 *Wbwd, const bf16 *mask, bf16 *dX, int *err, int sms,
+                      cudaStream_t s)
 {
-    launch_linear<kWidth, kWidth, EPI_MASK_BF16>(dZ, M, Wk, nullptr, mask, dX, err, sms, s);
+    launch_linear<kWidth, kWidth, EPI_MASK_BF16>(dZ, M, Wbwd, nullptr, mask, dX, err, sms, s);
 }
 
-void linear_back_heads(const bf16 *dZ, int M, const bf16 *Wk, const bf16 *mask, bf16 *dX, int n_out, int *err,
+void linear_back_mul(const bf16 *dZ, int M, const bf16 *Wbwd, const bf16 *mask, bf16 *dX, int *err, int sms,
+                     cudaStream_t s)
+{
+    launch_linear<kWidth, kWidth, EPI_MUL_BF16>(dZ, M, Wbwd, nullptr, mask, dX, err, sms, s);
+}
+
+void linear_back_heads(const bf16 *dZ, int M, const bf16 *Wbwd, const bf16 *mask, bf16 *dX, int n_out, int *err,
                        int sms, cudaStream_t s)
 {
     if (n_out == 16)
-        launch_linear<16, kWidth, EPI_MASK_BF16>(dZ, M, Wk, nullptr, mask, dX, err, sms, s);
+        launch_linear<16, kWidth, EPI_MASK_BF16>(dZ, M, Wbwd, nullptr, mask, dX, err, sms, s);
     else if (n_out == 32)
-        launch_linear<32, kWidth, EPI_MASK_BF16>(dZ, M, Wk, nullptr, mask, dX, err, sms, s);
+        launch_linear<32, kWidth, EPI_MASK_BF16>(dZ, M, Wbwd, nullptr, mask, dX, err, sms, s);
     else if (n_out == 64)
-        launch_linear<64, kWidth, EPI_MASK_BF16>(dZ, M, Wk, nullptr, mask, dX, err, sms, s);
+        launch_linear<64, kWidth, EPI_MASK_BF16>(dZ, M, Wbwd, nullptr, mask, dX, err, sms, s);
     else
         fail(CLODE_ERR_INVALID_ARGUMENT, "heads x outputs must be 16, 32 or 64 (got %d)", n_out);
 }
 
-void input_layer(const float *x, int M, const float *W1, const float *b1, bf16 *h1, cudaStream_t s)
+void input_layer(const float *x, int M, const float *W1, const float *b1, bf16 *h1, bf16 *c1, cudaStream_t s)
 {
-    k_input_layer<<<grid_for((size_t)M * kWidth), kThreads, 0, s>>>(x, M, W1, b1, h1);
+    k_input_layer<<<grid_for((size_t)tiled_rows(M) * (kWidth / 8)), kThreads, 0, s>>>(x, M, W1, b1, h1, c1);
     after_launch("input layer launch");
 }
 
 void mse(const float *out, const float *y, int M, int H, int K, bf16 *dz, float *loss, cudaStream_t s)
 {
-    k_mse<<<grid_for((size_t)M * H * K), kThreads, 0, s>>>(out, y, M, H, K, dz, loss);
+    k_mse<<<grid_for((size_t)tiled_rows(M) * (H * K / 8)), kThreads, 0, s>>>(out, y, M, H, K, dz, loss);
     after_launch("loss launch");
 }
 
-void weight_grad_bf16(const bf16 *A, int Kd, const bf16 *D, int N, int M, float *G, float *g, cudaStream_t s)
+namespace {
+int rows_per_block_for(int M, int max_blocks_z)
 {
-    dim3 grid((Kd + 15) / 16, (N + 15) / 16);
-    k_weight_grad<bf16><<<grid, 256, 0, s>>>(A, Kd, D, N, M, G, g);
+    int r = (M + max_blocks_z - 1) / max_blocks_z;
+    r = (r + 31) / 32 * 32;
+    return r < 64 ? 64 : r;
+}
+}  // namespace
+
+void weight_grad(const bf16 *A, int Kd, const bf16 *D, int N, int M, float *G, float *g, cudaStream_t s)
+{
+    if (M <= 0)
+        return;
+    const int rpb = rows_per_block_for(M, 8);
+    const unsigned int gz = (unsigned int)((M + rpb - 1) / rpb);
+    if (N % 64 == 0) {
+        dim3 grid((Kd + 63) / 64, N / 64, gz);
+        k_weight_grad<64><<<grid, 256, 0, s>>>(A, Kd, D, N, M, rpb, G, g);
+    } else {
+        dim3 grid((Kd + 63) / 64, (N + 15) / 16, gz);
+        k_weight_grad<16><<<grid, 256, 0, s>>>(A, Kd, D, N, M, rpb, G, g);
+    }
     after_launch("weight gradient launch");
 }
 
-void weight_grad_f32(const float *A, int Kd, const bf16 *D, int N, int M, float *G, float *g, cudaStream_t s)
+void weight_grad_input(const float *x, const bf16 *D, int M, float *G, float *g, cudaStream_t s)
 {
-    dim3 grid((Kd + 15) / 16, (N + 15) / 16);
-    k_weight_grad<float><<<grid, 256, 0, s>>>(A, Kd, D, N, M, G, g);
-    after_launch("weight gradient launch");
+    if (M <= 0)
+        return;
+    const int rpb = rows_per_block_for(M, 64);
+    k_weight_grad_input<<<(unsigned int)((M + rpb - 1) / rpb), kWidth, 0, s>>>(x, D, M, rpb, G, g);
+    after_launch("input-layer gradient launch");
 }
 
-void adam(float *w, const float *grad, float *m1, float *m2, int rows, int cols, float lr, const int *step,
-          bf16 *wt, bf16 *wk, cudaStream_t s)
+void adam_all(float *w, const float *grad, float *m1, float *m2, size_t n, float lr, const int *step,
+              const WeightImages *img, int n_img, int *cursor, const float *loss, float *loss_hist, int *hist_index,
+              cudaStream_t s)
 {
-    k_adam<<<grid_for((size_t)rows * cols), kThreads, 0, s>>>(w, grad, m1, m2, rows, cols, lr, 0.9f, 0.999f, 1e-8f,
-                                                              step, wt, wk);
+    k_adam_all<<<grid_for(n), kThreads, 0, s>>>(w, grad, m1, m2, n, lr, 0.9f, 0.999f, 1e-8f, step,
+                                                image_set(img, n_img), cursor, loss, loss_hist, hist_index);
     after_launch("Adam launch");
 }
 
-void step_increment(int *step, cudaStream_t s)
+void write_images(const float *w, const WeightImages *img, int n_img, cudaStream_t s)
 {
-    k_step_increment<<<1, 1, 0, s>>>(step);
-    after_launch("step counter launch");
+    size_t n = 0;
+    for (int i = 0; i < n_img; ++i)
+        n = n > img[i].offset + (size_t)img[i].k_in * img[i].n_out ? n : img[i].offset + (size_t)img[i].k_in * img[i].n_out;
+    k_write_images<<<grid_for(n), kThreads, 0, s>>>(w, image_set(img, n_img), n);
+    after_launch("weight image launch");
 }
 
-void gather_batch(const float *xs, const float *ys, int n_rows, int K, int B, int *cursor, float *xb, float *yb,
-                  cudaStream_t s)
+void gather_batch(const float *xs, const float *ys, int n_rows, int K, int B, const int *cursor, float *xb, float *yb,
+                  int *step, float *loss, cudaStream_t s)
 {
-    k_gather_batch<<<grid_for((size_t)B), kThreads, 0, s>>>(xs, ys, n_rows, K, B, cursor, xb, yb);
+    k_gather_batch<<<grid_for((size_t)B), kThreads, 0, s>>>(xs, ys, n_rows, K, B, cursor, xb, yb, step, loss);
     after_launch("batch gather launch");
-}
-
-void cursor_increment(int *cursor, cudaStream_t s)
-{
-    k_cursor_increment<<<1, 1, 0, s>>>(cursor);
-    after_launch("cursor launch");
 }
 
 void head_stats(const float *out, long long M, int H, int K, float *mean, float *spread, cudaStream_t s)

@@ -1,7 +1,8 @@
 // The surrogate network object behind the clode_mlp_* entry points: FP32
-// master parameters with Adam moments, BF16 copies of the tensor-core layer
+// master parameters with Adam moments, BF16 images of the tensor-core layer
 // weights in both operand orders, the training data resident on the device,
-// and one training step captured as a CUDA graph and replayed.
+// and one training step (13 kernels and a memset) captured as a CUDA graph
+// and replayed.
 //
 // Parameter vector layout (FP32, row-major [in x out]):
 //   W1 [2 x 256], b1 [256], W2 [256 x 256], b2 [256], W3 [256 x 256], b3 [256],
@@ -64,12 +65,13 @@ struct clode_mlp {
     // offsets into the parameter vector
     size_t oW1, ob1, oW2, ob2, oW3, ob3, oWh, obh, n_params;
     Buf params, grads, m1, m2;
-    Buf wt2, wk2, wt3, wk3, wth, wkh;  // BF16 operand copies
-    // batch work buffers (capacity cap rows)
+    Buf wf2, wb2, wf3, wb3, wfh, wbh;  // BF16 operand images (forward / backward order)
+    mlp::WeightImages images[3];
+    // batch work buffers (capacity cap rows, whole 128-row tiles)
     int cap = 0;
-    Buf xb, yb, h1, h2, h3, out, dzo, dz3, dz2, dz1;
+    Buf xb, yb, h1, c1, h2, h3, out, dzo, dz3, dz2, dz1;
     // training data and counters
-    Buf xs, ys, counters, loss_hist;  // counters: [0] step, [1] cursor, [2] error flag; loss accumulator after
+    Buf xs, ys, counters, loss_hist;  // counters: [0] step, [1] cursor, [2] error flag, [3] loss, [4] history index
     long long data_rows = 0;
     // prediction results
     Buf pred_mean, pred_spread;
@@ -77,16 +79,25 @@ struct clode_mlp {
     Buf thr, flags;
     double train_ms = 0, predict_ms = 0;
     cudaGraphExec_t graph = nullptr;
-    int graph_batch = 0;
-    float graph_lr = 0;
+    // what the captured training step baked in
+    struct GraphKey {
+        int batch = 0;
+        float lr = 0;
+        long long rows = 0;
+        const void *xs = nullptr, *ys = nullptr, *hist = nullptr;
+        bool operator==(const GraphKey &o) const
+        {
+            return batch == o.batch && lr == o.lr && rows == o.rows && xs == o.xs && ys == o.ys && hist == o.hist;
+        }
+    } graph_key;
 
     ~clode_mlp()
     {
         cudaSetDevice(device);
         if (graph)
             cudaGraphExecDestroy(graph);
-        for (Buf *b : {&params, &grads, &m1, &m2, &wt2, &wk2, &wt3, &wk3, &wth, &wkh, &xb, &yb, &h1, &h2, &h3, &out,
-                       &dzo, &dz3, &dz2, &dz1, &xs, &ys, &counters, &loss_hist, &pred_mean, &pred_spread, &thr,
+        for (Buf *b : {&params, &grads, &m1, &m2, &wf2, &wb2, &wf3, &wb3, &wfh, &wbh, &xb, &yb, &h1, &c1, &h2, &h3,
+                       &out, &dzo, &dz3, &dz2, &dz1, &xs, &ys, &counters, &loss_hist, &pred_mean, &pred_spread, &thr,
                        &flags})
             b->release();
         if (stream)
@@ -99,6 +110,7 @@ struct clode_mlp {
     int *cursor_ctr() const { return counters.as<int>() + 1; }
     int *err_flag() const { return counters.as<int>() + 2; }
     float *loss_acc() const { return (float *)(counters.as<int>() + 3); }
+    int *hist_index() const { return counters.as<int>() + 4; }
 
     void init(int k, int h, int dev, unsigned long long seed)
     {
@@ -124,15 +136,18 @@ struct clode_mlp {
         grads.reserve(n_params * 4);
         m1.reserve(n_params * 4);
         m2.reserve(n_params * 4);
-        wt2.reserve((size_t)kWidth * kWidth * 2);
-        wk2.reserve((size_t)kWidth * kWidth * 2);
-        wt3.reserve((size_t)kWidth * kWidth * 2);
-        wk3.reserve((size_t)kWidth * kWidth * 2);
-        wth.reserve((size_t)kWidth * HK * 2);
-        wkh.reserve((size_t)kWidth * HK * 2);
+        for (Buf *b : {&wf2, &wb2, &wf3, &wb3})
+            b->reserve((size_t)kWidth * kWidth * 2);
+        wfh.reserve((size_t)kWidth * HK * 2);
+        wbh.reserve((size_t)kWidth * HK * 2);
+        images[0] = {oW2, kWidth, kWidth, wf2.as<bf16>(), wb2.as<bf16>()};
+        images[1] = {oW3, kWidth, kWidth, wf3.as<bf16>(), wb3.as<bf16>()};
+        images[2] = {oWh, kWidth, HK, wfh.as<bf16>(), wbh.as<bf16>()};
         counters.reserve(64);
         check_cuda(cudaMemset(counters.p, 0, 64), "counters");
-        // He-uniform initial weights (ReLU layers), uniform 1/sqrt(fan_in) heads, zero biases
+        // first layer: frequencies U(-kInputScale, kInputScale) and phases
+        // U(-pi, pi) of the sine encoding; He-uniform ReLU layers; uniform
+        // 1/sqrt(fan_in) heads; zero biases elsewhere
         std::mt19937_64 gen(seed);
         std::vector<float> w(n_params, 0.0f);
         auto fill = [&](size_t off, size_t n, double a) {
@@ -140,37 +155,27 @@ struct clode_mlp {
             for (size_t i = 0; i < n; ++i)
                 w[off + i] = (float)d(gen);
         };
-        fill(oW1, 2 * kWidth, std::sqrt(6.0 / 2));
+        fill(oW1, 2 * kWidth, kInputScale);
+        fill(ob1, kWidth, 3.14159265358979);
         fill(oW2, (size_t)kWidth * kWidth, std::sqrt(6.0 / kWidth));
         fill(oW3, (size_t)kWidth * kWidth, std::sqrt(6.0 / kWidth));
         fill(oWh, (size_t)kWidth * HK, std::sqrt(1.0 / kWidth));
         set_params(w.data());
     }
 
-    // upload FP32 parameters, refresh the BF16 copies, reset Adam
+    static constexpr double kInputScale = 20.0;
+
+    // upload FP32 parameters, rebuild the BF16 images, reset Adam
     void set_params(const float *w)
     {
         use_device(device);
         check_cuda(cudaMemcpy(params.p, w, n_params * 4, cudaMemcpyHostToDevice), "parameters upload");
         check_cuda(cudaMemset(m1.p, 0, n_params * 4), "moments");
         check_cuda(cudaMemset(m2.p, 0, n_params * 4), "moments");
-        std::vector<bf16> t2((size_t)kWidth * kWidth), k2((size_t)kWidth * kWidth);
-        auto copies = [&](size_t off, int rows, int cols, Buf &wt, Buf &wk) {
-            std::vector<bf16> t((size_t)rows * cols), kk((size_t)rows * cols);
-            for (int r = 0; r < rows; ++r)
-                for (int c = 0; c < cols; ++c) {
-                    bf16 v = __float2bfloat16_rn(w[off + (size_t)r * cols + c]);
-                    t[(size_t)c * rows + r] = v;
-                    kk[(size_t)r * cols + c] = v;
-                }
-            check_cuda(cudaMemcpy(wt.p, t.data(), t.size() * 2, cudaMemcpyHostToDevice), "weights upload");
-            check_cuda(cudaMemcpy(wk.p, kk.data(), kk.size() * 2, cudaMemcpyHostToDevice), "weights upload");
-        };
-        copies(oW2, kWidth, kWidth, wt2, wk2);
-        copies(oW3, kWidth, kWidth, wt3, wk3);
-        copies(oWh, kWidth, HK, wth, wkh);
+        mlp::write_images(params.as<float>(), images, 3, stream);
         int zero = 0;
-        check_cuda(cudaMemcpy(step_ctr(), &zero, sizeof zero, cudaMemcpyHostToDevice), "counters");
+        check_cuda(cudaMemcpyAsync(step_ctr(), &zero, sizeof zero, cudaMemcpyHostToDevice, stream), "counters");
+        check_cuda(cudaStreamSynchronize(stream), "parameters upload");
     }
 
     void ensure_capacity(int rows)
@@ -178,62 +183,44 @@ struct clode_mlp {
         if (rows <= cap)
             return;
         cap = rows;
-        xb.reserve((size_t)rows * 2 * 4);
-        yb.reserve((size_t)rows * K * 4);
-        for (Buf *b : {&h1, &h2, &h3, &dz3, &dz2, &dz1})
-            b->reserve((size_t)rows * kWidth * 2);
-        out.reserve((size_t)rows * HK * 4);
-        dzo.reserve((size_t)rows * HK * 2);
+        const size_t tr = (size_t)mlp::tiled_rows(rows);
+        xb.reserve(tr * 2 * 4);
+        yb.reserve(tr * K * 4);
+        for (Buf *b : {&h1, &c1, &h2, &h3, &dz3, &dz2, &dz1})
+            b->reserve(tr * kWidth * 2);
+        out.reserve(tr * HK * 4);
+        dzo.reserve(tr * HK * 2);
         if (graph) {
             cudaGraphExecDestroy(graph);
             graph = nullptr;
         }
     }
 
-    // forward on the rows in xb -> h1, h2, h3, out
+    // forward on the rows in xb -> h1 (sine), h2, h3, out
     void forward(int rows)
     {
-        mlp::input_layer(xb.as<float>(), rows, P(oW1), P(ob1), h1.as<bf16>(), stream);
-        mlp::linear_relu(h1.as<bf16>(), rows, wt2.as<bf16>(), P(ob2), h2.as<bf16>(), err_flag(), sms, stream);
-        mlp::linear_relu(h2.as<bf16>(), rows, wt3.as<bf16>(), P(ob3), h3.as<bf16>(), err_flag(), sms, stream);
-        mlp::linear_heads(h3.as<bf16>(), rows, wth.as<bf16>(), P(obh), out.as<float>(), HK, err_flag(), sms, stream);
+        mlp::input_layer(xb.as<float>(), rows, P(oW1), P(ob1), h1.as<bf16>(), c1.as<bf16>(), stream);
+        mlp::linear_relu(h1.as<bf16>(), rows, wf2.as<bf16>(), P(ob2), h2.as<bf16>(), err_flag(), sms, stream);
+        mlp::linear_relu(h2.as<bf16>(), rows, wf3.as<bf16>(), P(ob3), h3.as<bf16>(), err_flag(), sms, stream);
+        mlp::linear_heads(h3.as<bf16>(), rows, wfh.as<bf16>(), P(obh), out.as<float>(), HK, err_flag(), sms, stream);
     }
 
-    // loss and gradients of the batch in xb / yb into grads
+    // loss and gradients of the batch in xb / yb into grads (the loss
+    // accumulator must be zero on entry)
     void backward(int rows)
     {
+        check_cuda(cudaMemsetAsync(grads.p, 0, n_params * 4, stream), "gradient reset");
         mlp::mse(out.as<float>(), yb.as<float>(), rows, H, K, dzo.as<bf16>(), loss_acc(), stream);
-        mlp::weight_grad_bf16(h3.as<bf16>(), kWidth, dzo.as<bf16>(), HK, rows, G(oWh), G(obh), stream);
-        mlp::linear_back_heads(dzo.as<bf16>(), rows, wkh.as<bf16>(), h3.as<bf16>(), dz3.as<bf16>(), HK, err_flag(),
+        mlp::weight_grad(h3.as<bf16>(), kWidth, dzo.as<bf16>(), HK, rows, G(oWh), G(obh), stream);
+        mlp::linear_back_heads(dzo.as<bf16>(), rows, wbh.as<bf16>(), h3.as<bf16>(), dz3.as<bf16>(), HK, err_flag(),
                                sms, stream);
-        mlp::weight_grad_bf16(h2.as<bf16>(), kWidth, dz3.as<bf16>(), kWidth, rows, G(oW3), G(ob3), stream);
-        mlp::linear_back_hidden(dz3.as<bf16>(), rows, wk3.as<bf16>(), h2.as<bf16>(), dz2.as<bf16>(), err_flag(), sms,
-                                stream);
-        mlp::weight_grad_bf16(h1.as<bf16>(), kWidth, dz2.as<bf16>(), kWidth, rows, G(oW2), G(ob2), stream);
-        mlp::linear_back_hidden(dz2.as<bf16>(), rows, wk2.as<bf16>(), h1.as<bf16>(), dz1.as<bf16>(), err_flag(), sms,
-                                stream);
-        mlp::weight_grad_f32(xb.as<float>(), 2, dz1.as<bf16>(), kWidth, rows, G(oW1), G(ob1), stream);
-    }
-
-    void adam_all(float lr)
-    {
-        mlp::step_increment(step_ctr(), stream);
-        mlp::adam(P(oW1), G(oW1), m1.as<float>() + oW1, m2.as<float>() + oW1, 2, kWidth, lr, step_ctr(), nullptr,
-                  nullptr, stream);
-        mlp::adam(P(ob1), G(ob1), m1.as<float>() + ob1, m2.as<float>() + ob1, 1, kWidth, lr, step_ctr(), nullptr,
-                  nullptr, stream);
-        mlp::adam(P(oW2), G(oW2), m1.as<float>() + oW2, m2.as<float>() + oW2, kWidth, kWidth, lr, step_ctr(),
-                  wt2.as<bf16>(), wk2.as<bf16>(), stream);
-        mlp::adam(P(ob2), G(ob2), m1.as<float>() + ob2, m2.as<float>() + ob2, 1, kWidth, lr, step_ctr(), nullptr,
-                  nullptr, stream);
-        mlp::adam(P(oW3), G(oW3), m1.as<float>() + oW3, m2.as<float>() + oW3, kWidth, kWidth, lr, step_ctr(),
-                  wt3.as<bf16>(), wk3.as<bf16>(), stream);
-        mlp::adam(P(ob3), G(ob3), m1.as<float>() + ob3, m2.as<float>() + ob3, 1, kWidth, lr, step_ctr(), nullptr,
-                  nullptr, stream);
-        mlp::adam(P(oWh), G(oWh), m1.as<float>() + oWh, m2.as<float>() + oWh, kWidth, HK, lr, step_ctr(),
-                  wth.as<bf16>(), wkh.as<bf16>(), stream);
-        mlp::adam(P(obh), G(obh), m1.as<float>() + obh, m2.as<float>() + obh, 1, HK, lr, step_ctr(), nullptr,
-                  nullptr, stream);
+        mlp::weight_grad(h2.as<bf16>(), kWidth, dz3.as<bf16>(), kWidth, rows, G(oW3), G(ob3), stream);
+        mlp::linear_back_relu(dz3.as<bf16>(), rows, wb3.as<bf16>(), h2.as<bf16>(), dz2.as<bf16>(), err_flag(), sms,
+                              stream);
+        mlp::weight_grad(h1.as<bf16>(), kWidth, dz2.as<bf16>(), kWidth, rows, G(oW2), G(ob2), stream);
+        mlp::linear_back_mul(dz2.as<bf16>(), rows, wb2.as<bf16>(), c1.as<bf16>(), dz1.as<bf16>(), err_flag(), sms,
+                             stream);
+        mlp::weight_grad_input(xb.as<float>(), dz1.as<bf16>(), rows, G(oW1), G(ob1), stream);
     }
 
     void check_error_flag()
@@ -241,7 +228,7 @@ struct clode_mlp {
         int e = 0;
         check_cuda(cudaMemcpy(&e, err_flag(), sizeof e, cudaMemcpyDeviceToHost), "error flag");
         if (e)
-            fail(CLODE_ERR_CUDA, "a tensor-core layer timed out waiting for its MMA group (results invalid)");
+            fail(CLODE_ERR_CUDA, "a tensor-core layer timed out waiting for a copy or its MMA group (results invalid)");
     }
 
     void gradients(const float *x, const float *y, int rows, float *g_out, float *loss)
@@ -264,6 +251,8 @@ struct clode_mlp {
     {
         if (n < 1 || steps < 0 || batch < 1)
             fail(CLODE_ERR_INVALID_ARGUMENT, "train: need n >= 1, steps >= 0, batch >= 1");
+        if (n > 0x7FFFFFFFLL)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "train: at most 2^31 - 1 rows");
         use_device(device);
         // one shuffled copy of the data on the device; batches walk through it
         std::vector<long long> perm((size_t)n);
@@ -286,25 +275,31 @@ struct clode_mlp {
         data_rows = n;
         ensure_capacity(batch);
         loss_hist.reserve((size_t)(steps > 0 ? steps : 1) * 4);
-        int zero = 0;
-        check_cuda(cudaMemcpy(cursor_ctr(), &zero, sizeof zero, cudaMemcpyHostToDevice), "cursor");
+        check_cuda(cudaMemsetAsync(cursor_ctr(), 0, sizeof(int), stream), "cursor");
+        check_cuda(cudaMemsetAsync(hist_index(), 0, sizeof(int), stream), "history index");
 
         auto one_step = [&]() {
-            check_cuda(cudaMemsetAsync(loss_acc(), 0, 4, stream), "loss reset");
             mlp::gather_batch(xs.as<float>(), ys.as<float>(), (int)n, K, batch, cursor_ctr(), xb.as<float>(),
-                              yb.as<float>(), stream);
-            mlp::cursor_increment(cursor_ctr(), stream);
+                              yb.as<float>(), step_ctr(), loss_acc(), stream);
             forward(batch);
             backward(batch);
-            adam_all(lr);
+            mlp::adam_all(params.as<float>(), grads.as<float>(), m1.as<float>(), m2.as<float>(), n_params, lr,
+                          step_ctr(), images, 3, cursor_ctr(), loss_acc(), loss_hist.as<float>(), hist_index(),
+                          stream);
         };
         auto t0 = std::chrono::steady_clock::now();
         if (steps > 0) {
             // first step eagerly (sets kernel attributes), the rest as a replayed graph
             one_step();
-            check_cuda(cudaMemcpyAsync(loss_hist.p, loss_acc(), 4, cudaMemcpyDeviceToDevice, stream), "loss copy");
             if (steps > 1) {
-                if (!graph || graph_batch != batch || graph_lr != lr) {
+                GraphKey key;
+                key.batch = batch;
+                key.lr = lr;
+                key.rows = n;
+                key.xs = xs.p;
+                key.ys = ys.p;
+                key.hist = loss_hist.p;
+                if (!graph || !(graph_key == key)) {
                     if (graph) {
                         cudaGraphExecDestroy(graph);
                         graph = nullptr;
@@ -315,15 +310,11 @@ struct clode_mlp {
                     check_cuda(cudaStreamEndCapture(stream, &g), "graph capture");
                     check_cuda(cudaGraphInstantiate(&graph, g, 0), "graph instantiate");
                     cudaGraphDestroy(g);
-                    graph_batch = batch;
-                    graph_lr = lr;
+                    graph_key = key;
                 }
                 for (int s = 1; s < steps; ++s) {
                     check_cuda(cudaGraphLaunch(graph, stream), "graph launch");
                     count_launch();
-                    check_cuda(cudaMemcpyAsync(loss_hist.as<float>() + s, loss_acc(), 4, cudaMemcpyDeviceToDevice,
-                                               stream),
-                               "loss copy");
                 }
             }
         }

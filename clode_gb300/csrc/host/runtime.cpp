@@ -296,6 +296,8 @@ CompiledProgram compile_program(const ProgramSpec &spec)
         opts.push_back("-ftz=true");
     if (spec.maxrregcount > 0)
         opts.push_back("--maxrregcount=" + std::to_string(spec.maxrregcount));
+    if (spec.fast_math)
+        opts.push_back("--use_fast_math");
     for (auto &d : spec.defines)
         opts.push_back(d);
     std::string optline;

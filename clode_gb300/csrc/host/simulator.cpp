@@ -217,6 +217,7 @@ struct clode_sim {
     bool fmad = false;
     bool prec_div = true;
     bool ftz = false;
+    bool fast_math = false;
     int maxrregcount = 0;
     double time_budget_ms = 0.0;
     bool fuse_init = true;
@@ -332,6 +333,7 @@ struct clode_sim {
         s.prec_div = prec_div;
         s.ftz = ftz;
         s.maxrregcount = maxrregcount;
+        s.fast_math = fast_math;
         s.arch = device_arch(device);
         s.defines = {single ? "-DCLODE_SINGLE_PRECISION" : "-DCLODE_DOUBLE_PRECISION", "-D" + kSteppers.at(stepper),
                      "-DN_PAR=" + std::to_string(nPar), "-DN_VAR=" + std::to_string(nVar),
@@ -1490,9 +1492,9 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 sim->fmad = v;
                 sim->built = false;
             }
-        } else if (k == "prec_div" || k == "ftz") {
+        } else if (k == "prec_div" || k == "ftz" || k == "fast_math") {
             bool v = value != 0.0;
-            bool &field = k == "prec_div" ? sim->prec_div : sim->ftz;
+            bool &field = k == "prec_div" ? sim->prec_div : (k == "ftz" ? sim->ftz : sim->fast_math);
             if (v != field) {
                 field = v;
                 sim->built = false;
@@ -1529,6 +1531,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "fmad") *value = sim->fmad;
         else if (k == "prec_div") *value = sim->prec_div;
         else if (k == "ftz") *value = sim->ftz;
+        else if (k == "fast_math") *value = sim->fast_math;
         else if (k == "maxrregcount") *value = sim->maxrregcount;
         else if (k == "time_budget_ms") *value = sim->time_budget_ms;
         else if (k == "fuse_init") *value = sim->fuse_init;

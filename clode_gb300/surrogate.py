@@ -1,12 +1,13 @@
 """Learned surrogate for large feature maps (no counterpart in clODE).
 
-An MLP 2 -> 256 -> 256 -> 256 -> H heads x K features (BF16 tensor-core
-layers with FP32 accumulation, trained on the GPU by this package's own
-kernels, include/clode_gb300.h ``clode_mlp_*``) learns a feature map from a
-coarse sub-grid that the ensemble engine integrates.  It then predicts the
-full grid, and every point where the heads disagree or a feature jumps
-between grid neighbours is integrated again by the plain engine, which stays
-the fallback and the judge of the surrogate's error.
+An MLP 2 -> 256 (sine) -> 256 -> 256 -> H heads x K features (BF16
+tensor-core layers with FP32 accumulation, trained on the GPU by this
+package's own kernels, include/clode_gb300.h ``clode_mlp_*``) learns a
+feature map from a coarse sub-grid that the ensemble engine integrates.  It
+then predicts the full grid; the cells of the sub-grid where the network
+misses the integrated corners, or where the corners reveal a discontinuity,
+are integrated again by the plain engine, which stays the fallback and the
+judge of the surrogate's error.
 
 ``FeatureMapScreen.run`` is the whole workflow; ``MLP`` is the network.
 """
@@ -35,13 +36,24 @@ def _check(rc: int):
 class MLP:
     """The surrogate network on one GPU (handle of ``clode_mlp_create``)."""
 
-    def __init__(self, n_outputs: int = 4, n_heads: int = 4, device: int = 0, seed: int = 0):
+    WIDTH = 256
+
+    def __init__(self, n_outputs: int = 4, n_heads: int = 4, device: int = 0, seed: int = 0,
+                 input_scale: float | None = None):
+        """`input_scale`: the first (sine) layer's frequencies are drawn from
+        U(-input_scale, input_scale) for inputs normalised to [-1, 1]
+        (default: the library's, 20)."""
         self.K, self.H = n_outputs, n_heads
         self._h = C.c_void_p()
         _check(N.lib.clode_mlp_create(n_outputs, n_heads, device, seed, C.byref(self._h)))
         n = C.c_size_t(0)
         _check(N.lib.clode_mlp_param_count(self._h, C.byref(n)))
         self.n_params = n.value
+        if input_scale is not None:
+            p = self.get_params()
+            rng = np.random.default_rng(seed)
+            p[:2 * self.WIDTH] = rng.uniform(-input_scale, input_scale, 2 * self.WIDTH)
+            self.set_params(p)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -101,13 +113,19 @@ class MLP:
 @dataclass
 class ScreenResult:
     features: np.ndarray            # (ny*nx, K) screened map
-    flags: np.ndarray               # per point: 0 surrogate value kept, else re-integrated
+    flags: np.ndarray               # per point: SURROGATE, FALLBACK or SAMPLED
     timings: dict = field(default_factory=dict)
     loss: np.ndarray | None = None
 
+    SURROGATE, FALLBACK, SAMPLED = 0, 1, 2
+
     @property
     def fallback_fraction(self) -> float:
-        return float(np.mean(self.flags != 0))
+        return float(np.mean(self.flags == self.FALLBACK))
+
+    @property
+    def integrated_fraction(self) -> float:
+        return float(np.mean(self.flags != self.SURROGATE))
 
 
 class FeatureMapScreen:
@@ -116,14 +134,27 @@ class FeatureMapScreen:
     ``integrate(par0, par1) -> (n, K) features`` runs the plain engine on the
     given parameter points (a callable, so any model, stepper and observer
     can be screened).  ``lo``/``hi`` bound the two parameters.
+
+    Error measure: a point's error is the largest over the K features of
+    |surrogate - engine| / (the feature's range over the map), so "1 %" means
+    one percent of the feature's span.
+
+    Screening is by cells of the integrated sub-grid: a cell's points take
+    the network's values when the network reproduces the four integrated
+    corners to within ``r`` and the corners themselves vary by at most ``v``
+    (no discontinuity crosses the cell's corners); otherwise every point of
+    the cell is integrated.  ``r`` and ``v`` are calibrated on a random sample
+    of integrated interior points so that a fraction ``keep`` of the accepted
+    sample points is within ``tol``.
     """
 
-    def __init__(self, integrate, lo, hi, n_features: int, n_heads: int = 4, seed: int = 0, device: int = 0):
+    def __init__(self, integrate, lo, hi, n_features: int, n_heads: int = 4, seed: int = 0, device: int = 0,
+                 input_scale: float | None = None):
         self.integrate = integrate
         self.lo = np.asarray(lo, dtype=np.float64)
         self.hi = np.asarray(hi, dtype=np.float64)
         self.K = n_features
-        self.net = MLP(n_features, n_heads, device, seed)
+        self.net = MLP(n_features, n_heads, device, seed, input_scale=input_scale)
         self.seed = seed
 
     def _norm_x(self, p0, p1):
@@ -132,96 +163,104 @@ class FeatureMapScreen:
         return np.stack([x0, x1], axis=1).astype(np.float32)
 
     @staticmethod
-    def rel_error(F, ref, scale):
-        """Per point: the largest relative error over the features, relative to
-        |ref| + 1e-3 * (feature scale) so features crossing zero stay defined."""
-        return (np.abs(F - ref) / (np.abs(ref) + 1e-3 * scale)).max(axis=1)
+    def map_error(F, ref, scale):
+        """Per point: max over features of |F - ref| / scale (scale = feature range)."""
+        return (np.abs(np.asarray(F, np.float64) - ref) / np.maximum(scale, 1e-30)).max(axis=1)
 
-    def calibrate(self, Xv, Fv, mu, sd, dx, dy, scale, tol, keep):
-        """Thresholds on head spread and neighbour jump (normalised units) such
-        that, on held-out integrated points, at least `keep` of the points the
-        screen accepts have error <= tol; among those, the pair that accepts
-        the most points.  Returns (spread_thr, jump_thr, accepted fraction)."""
-        mean, spread = self.net.predict(Xv)
-        err = self.rel_error(mean.astype(np.float64) * sd + mu, Fv, scale)
-        s = spread.max(axis=1)
-        j = np.zeros_like(s)
-        for d in (np.array([dx, 0.0], np.float32), np.array([0.0, dy], np.float32)):
-            for sign in (1.0, -1.0):
-                mn, _ = self.net.predict(Xv + sign * d)
-                j = np.maximum(j, np.abs(mn - mean).max(axis=1))
-        qs = np.concatenate([np.linspace(0.0, 0.95, 20), [0.975, 0.99, 1.0]])
-        s_cand = np.quantile(s, qs)
-        j_cand = np.quantile(j, qs)
+    @staticmethod
+    def _calibrate(r, v, err, tol, keep):
+        """Thresholds (r_max, v_max) on the sample's cell statistics such that
+        at least `keep` of the accepted sample points have err <= tol; the pair
+        accepting the most points.  Returns (r_max, v_max, accepted fraction),
+        (-1, -1, 0) when no pair qualifies."""
+        qs = np.concatenate([np.linspace(0.0, 0.95, 39), [0.975, 0.99, 1.0]])
         best = (-1.0, -1.0, 0.0)
-        for ts in s_cand:
-            ok_s = s <= ts
-            for tj in j_cand:
-                acc = ok_s & (j <= tj)
-                frac = acc.mean()
+        good = err <= tol
+        for tr in np.unique(np.quantile(r, qs)):
+            ok_r = r <= tr
+            for tv in np.unique(np.quantile(v, qs)):
+                acc = ok_r & (v <= tv)
+                frac = float(acc.mean())
                 if frac <= best[2] or not acc.any():
                     continue
-                if np.mean(err[acc] <= tol) >= keep:
-                    best = (float(ts), float(tj), float(frac))
+                if good[acc].mean() >= keep:
+                    best = (float(tr), float(tv), frac)
         return best
 
     def run(self, nx: int, ny: int, train_stride: int = 8, steps: int = 3000, batch: int = 4096,
-            lr: float = 2e-3, tol: float = 0.01, keep: float = 0.99, holdout: float = 0.1) -> ScreenResult:
-        """Screened map of the nx x ny grid; `tol`/`keep`: the accepted
-        surrogate values are calibrated to have error <= tol for a fraction
-        `keep` of held-out integrated points."""
+            lr: float = 2e-3, tol: float = 0.01, keep: float = 0.99, n_calibration: int = 65536) -> ScreenResult:
+        """Screened map of the nx x ny grid (point m = iy * nx + ix)."""
         t_all = time.perf_counter()
         g0 = np.linspace(self.lo[0], self.hi[0], nx)
         g1 = np.linspace(self.lo[1], self.hi[1], ny)
-        P0, P1 = np.meshgrid(g0, g1, indexing="xy")  # point m = iy * nx + ix
-        P0, P1 = P0.ravel(), P1.ravel()
-        # 1. a coarse sub-grid integrated by the engine
-        sub = np.zeros((ny, nx), dtype=bool)
-        sub[::train_stride, ::train_stride] = True
-        sub = sub.ravel()
+        # 1. the sub-grid (every train_stride-th line and the last one) integrated by the engine
+        sx = np.unique(np.r_[0:nx:train_stride, nx - 1])
+        sy = np.unique(np.r_[0:ny:train_stride, ny - 1])
+        SX, SY = np.meshgrid(sx, sy, indexing="xy")
+        sub = (SY * nx + SX).ravel()
         t0 = time.perf_counter()
-        Fsub = np.asarray(self.integrate(P0[sub], P1[sub]), dtype=np.float64)
+        Fsub = np.asarray(self.integrate(g0[SX.ravel()], g1[SY.ravel()]), dtype=np.float64)
         t_train_data = time.perf_counter() - t0
-        Xsub = self._norm_x(P0[sub], P1[sub])
-        rng = np.random.default_rng(self.seed)
-        val = rng.random(Xsub.shape[0]) < holdout
-        mu, sd = Fsub[~val].mean(axis=0), Fsub[~val].std(axis=0) + 1e-12
-        scale = np.abs(Fsub).max(axis=0)
-        Y = ((Fsub[~val] - mu) / sd).astype(np.float32)
+        lo, hi = Fsub.min(axis=0), Fsub.max(axis=0)
+        scale = np.maximum(hi - lo, 1e-30)
+        mu, sd = (hi + lo) / 2.0, scale / 2.0
+        Xsub = self._norm_x(g0[SX.ravel()], g1[SY.ravel()])
+        Y = ((Fsub - mu) / sd).astype(np.float32)
         # 2. training on the GPU, learning rate halved over four phases
         t0 = time.perf_counter()
-        losses = []
-        for ph in range(4):
-            losses.append(self.net.train(Xsub[~val], Y, steps=steps // 4, batch=batch, lr=lr / 2 ** ph,
-                                         seed=self.seed + ph))
+        losses = [self.net.train(Xsub, Y, steps=steps // 4, batch=batch, lr=lr / 2 ** ph, seed=self.seed + ph)
+                  for ph in range(4)]
         loss = np.concatenate(losses)
         t_train = time.perf_counter() - t0
-        # 3. calibration of the screen on the held-out integrated points
+        # 3. prediction of the full grid
         t0 = time.perf_counter()
-        dx, dy = 2.0 / max(nx - 1, 1), 2.0 / max(ny - 1, 1)
-        ts, tj, acc = self.calibrate(Xsub[val], Fsub[val], mu, sd, dx, dy, scale, tol, keep)
-        t_cal = time.perf_counter() - t0
-        # 4. prediction of the full grid and screening
-        t0 = time.perf_counter()
-        mean, spread = self.net.predict(self._norm_x(P0, P1))
-        flags = self.net.screen(nx, ny, np.full(self.K, ts), np.full(self.K, tj))
-        if ts < 0:
-            flags[:] = 4  # no threshold met the error bar: everything is integrated
-        t_predict = time.perf_counter() - t0
+        PX, PY = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+        mean, _ = self.net.predict(self._norm_x(g0[PX.ravel()], g1[PY.ravel()]))
         F = mean.astype(np.float64) * sd + mu
-        # the integrated sub-grid points are known exactly
-        F[sub] = Fsub
-        flags[sub] = 0
-        # 4. fallback: the plain engine on every flagged point
+        t_predict = time.perf_counter() - t0
+        # 4. cell statistics from the integrated corners
         t0 = time.perf_counter()
-        redo = np.nonzero(flags)[0]
+        Fs = Fsub.reshape(sy.size, sx.size, self.K)
+        Ps = F.reshape(ny, nx, self.K)[np.ix_(sy, sx)]
+        R = (np.abs(Ps - Fs) / scale).max(axis=2)
+        r_cell = np.maximum.reduce([R[:-1, :-1], R[:-1, 1:], R[1:, :-1], R[1:, 1:]]) if R.shape[0] > 1 and R.shape[1] > 1 \
+            else np.zeros((0, 0))
+        cmax = np.maximum.reduce([Fs[:-1, :-1], Fs[:-1, 1:], Fs[1:, :-1], Fs[1:, 1:]])
+        cmin = np.minimum.reduce([Fs[:-1, :-1], Fs[:-1, 1:], Fs[1:, :-1], Fs[1:, 1:]])
+        v_cell = ((cmax - cmin) / scale).max(axis=2)
+        cx = np.clip(np.searchsorted(sx, np.arange(nx), side="right") - 1, 0, sx.size - 2)
+        cy = np.clip(np.searchsorted(sy, np.arange(ny), side="right") - 1, 0, sy.size - 2)
+        r_pt = r_cell[cy[:, None], cx[None, :]].ravel()
+        v_pt = v_cell[cy[:, None], cx[None, :]].ravel()
+        flags = np.full(nx * ny, ScreenResult.SURROGATE, dtype=np.int8)
+        flags[sub] = ScreenResult.SAMPLED
+        F[sub] = Fsub
+        t_cells = time.perf_counter() - t0
+        # 5. calibration sample: random interior points, integrated exactly
+        t0 = time.perf_counter()
+        rng = np.random.default_rng(self.seed + 101)
+        interior = np.nonzero(flags == ScreenResult.SURROGATE)[0]
+        cal = rng.choice(interior, size=min(n_calibration, interior.size), replace=False) if interior.size else \
+            np.zeros(0, dtype=np.int64)
+        Fcal = np.asarray(self.integrate(g0[cal % nx], g1[cal // nx]), dtype=np.float64) if cal.size else \
+            np.zeros((0, self.K))
+        tr, tv, acc = self._calibrate(r_pt[cal], v_pt[cal], self.map_error(F[cal], Fcal, scale), tol, keep) \
+            if cal.size else (-1.0, -1.0, 0.0)
+        F[cal] = Fcal
+        flags[cal] = ScreenResult.SAMPLED
+        t_cal = time.perf_counter() - t0
+        # 6. fallback: the plain engine on every point of a rejected cell
+        t0 = time.perf_counter()
+        reject = (flags == ScreenResult.SURROGATE) & ((r_pt > tr) | (v_pt > tv))
+        redo = np.nonzero(reject)[0]
         if redo.size:
-            F[redo] = np.asarray(self.integrate(P0[redo], P1[redo]), dtype=np.float64)
+            F[redo] = np.asarray(self.integrate(g0[redo % nx], g1[redo // nx]), dtype=np.float64)
+            flags[redo] = ScreenResult.FALLBACK
         t_fallback = time.perf_counter() - t0
         total = time.perf_counter() - t_all
         return ScreenResult(F, flags, loss=loss, timings={
-            "train_data_s": t_train_data, "train_s": t_train, "calibrate_s": t_cal, "predict_screen_s": t_predict,
-            "fallback_s": t_fallback, "total_s": total, "points": nx * ny,
-            "points_per_s": nx * ny / total, "fallback_points": int(redo.size),
-            "integrated_points": int(redo.size + sub.sum()), "spread_thr": ts, "jump_thr": tj,
-            "calibrated_accept_fraction": acc})
+            "train_data_s": t_train_data, "train_s": t_train, "predict_s": t_predict, "cells_s": t_cells,
+            "calibrate_s": t_cal, "fallback_s": t_fallback, "total_s": total, "points": nx * ny,
+            "points_per_s": nx * ny / total, "training_points": int(sub.size), "calibration_points": int(cal.size),
+            "fallback_points": int(redo.size), "integrated_points": int(np.count_nonzero(flags)),
+            "r_max": tr, "v_max": tv, "calibrated_accept_fraction": acc, "feature_scale": scale.tolist()})
