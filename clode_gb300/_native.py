@@ -140,6 +140,8 @@ SIGNATURES = {
                                   C.c_float, C.c_ulonglong, C.POINTER(C.c_float)]),
     "clode_mlp_predict": (C.c_int, [_P, C.POINTER(C.c_float), C.c_longlong, C.POINTER(C.c_float),
                                     C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "clode_mlp_predict_grid": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                          C.POINTER(C.c_float)]),
     "clode_mlp_screen": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                    C.POINTER(C.c_int)]),
     "clode_mlp_timings": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

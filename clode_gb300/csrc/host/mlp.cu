@@ -15,8 +15,9 @@
 // tile arrive in shared memory by one bulk asynchronous copy each
 // (cp.async.bulk, completion on an mbarrier), and the next tile's copy is
 // issued as soon as the MMA group has consumed the current one.  Weight
-// gradients (X^T dZ over the batch), the 2-wide input layer, the loss and
-// Adam are small and run on the CUDA cores.
+// gradients (X^T dZ, a reduction over the batch) run on the tensor cores too,
+// reading the same tiles as MN-major operands.  The 2-wide input layer, its
+// gradient, the loss and Adam are small and run on the CUDA cores.
 //
 // Every wait on an mbarrier is bounded: one thread polls with an iteration
 // limit, publishes the outcome through shared memory, and on a timeout the
@@ -248,7 +249,13 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
         for (int c0 = 0; c0 < N; c0 += 16) {
             float v[16];
             tmem_ld16(trow + (uint32_t)c0, v);
-            if (m < M) {
+            if (m >= M && EPI != EPI_BIAS_F32) {
+                // rows past M in the last tile are zero, so that batch
+                // reductions over whole tiles see nothing there
+                bf16 *y = (bf16 *)Y;
+                *(uint4 *)(y + tiled_offset(m, c0, N)) = make_uint4(0u, 0u, 0u, 0u);
+                *(uint4 *)(y + tiled_offset(m, c0 + 8, N)) = make_uint4(0u, 0u, 0u, 0u);
+            } else if (m < M) {
                 if (EPI == EPI_BIAS_F32) {
                     float *y = (float *)Y + (size_t)m * N + c0;
 #pragma unroll
@@ -343,8 +350,12 @@ __global__ void k_input_layer(const float *__restrict__ x, int M, const float *_
         long long m;
         int c8;
         chunk_coords(idx, kWidth, m, c8);
-        if (m >= M)
+        const size_t o = tiled_offset(m, c8 * 8, kWidth);
+        if (m >= M) {  // zero padding rows of the last tile
+            *(uint4 *)(h1 + o) = make_uint4(0u, 0u, 0u, 0u);
+            *(uint4 *)(c1 + o) = make_uint4(0u, 0u, 0u, 0u);
             continue;
+        }
         const float x0 = x[2 * m], x1 = x[2 * m + 1];
         __align__(16) bf16 hs[8], hc[8];
 #pragma unroll
@@ -356,7 +367,6 @@ __global__ void k_input_layer(const float *__restrict__ x, int M, const float *_
             hs[j] = __float2bfloat16_rn(sz);
             hc[j] = __float2bfloat16_rn(cz);
         }
-        const size_t o = tiled_offset(m, c8 * 8, kWidth);
         *(uint4 *)(h1 + o) = *(const uint4 *)hs;
         *(uint4 *)(c1 + o) = *(const uint4 *)hc;
     }
@@ -377,8 +387,10 @@ __global__ void k_mse(const float *__restrict__ out, const float *__restrict__ y
         long long m;
         int c8;
         chunk_coords(idx, HK, m, c8);
-        if (m >= M)
+        if (m >= M) {  // zero padding rows of the last tile
+            *(uint4 *)(dz + tiled_offset(m, c8 * 8, HK)) = make_uint4(0u, 0u, 0u, 0u);
             continue;
+        }
         __align__(16) bf16 o[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
@@ -395,98 +407,163 @@ __global__ void k_mse(const float *__restrict__ out, const float *__restrict__ y
         atomicAdd(loss, local / ((float)M * (float)HK));
 }
 
-// weight gradient over one chunk of batch rows:
-//   G[k, n] += sum_m A[m, k] D[m, n],  g[n] += sum_m D[m, n]  (g from the k0 = 0 blocks)
-// A: BF16 [M x Kd], D: BF16 [M x N], both core-matrix order.  A block owns a
-// 64 x TN output tile and rows [z * rows_per_block, ...); 256 threads, each
-// 4 x (TN / 16) outputs.
-template <int TN>
-__global__ void __launch_bounds__(256) k_weight_grad(const bf16 *__restrict__ A, int Kd, const bf16 *__restrict__ D,
-                                                     int N, int M, int rows_per_block, float *__restrict__ G,
-                                                     float *__restrict__ g)
+// instruction descriptor with operand majors: a_mn / b_mn select MN-major A / B
+__host__ __device__ constexpr uint32_t idesc_bf16_major(int M, int N, bool a_mn, bool b_mn)
 {
-    constexpr int TK = 64, RM = 32, RN = TN / 16;
-    __shared__ __align__(16) float sa[RM][TK];
-    __shared__ __align__(16) float sd[RM][TN];
-    const int k0 = blockIdx.x * TK, n0 = blockIdx.y * TN;
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int m_begin = blockIdx.z * rows_per_block;
-    const int m_end = min(M, m_begin + rows_per_block);
-    float acc[4][RN];
-    float bacc[RN];
+    return idesc_bf16(M, N) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
+}
+
+// A core-matrix-order tile (W wide, rows = the reduction) read as an MN-major
+// operand: 8-row groups along K are W * 16 bytes apart (LBO), core matrices
+// along MN 128 bytes apart (SBO)
+__device__ __forceinline__ uint64_t smem_desc_mn(uint32_t addr, int W) { return smem_desc(addr, (uint32_t)W * 16u, 128u); }
+
+// Weight gradient on the tensor cores:
+//   G[k, n] += sum_m A[m, k] D[m, n]   (k in this CTA's half of A's 256 columns)
+//   g[n]    += sum_m D[m, n]           (half 0; an MMA against an all-ones operand)
+// A: BF16 [M x 256], D: BF16 [M x N], core-matrix order with zero rows past M.
+// The batch is the reduction: each 128-row tile of A and D is read as an
+// MN-major operand straight from its bulk copy, 8 K-steps of 16 rows,
+// accumulating in tensor memory over this CTA's tiles; the sums are added
+// into G and g with vector atomics.  Grid: 2 halves x batch splits.
+template <int N>
+__global__ void __launch_bounds__(128, 1) k_wgrad_tc(const bf16 *__restrict__ A, const bf16 *__restrict__ D, int M,
+                                                      int tiles_per_cta, float *__restrict__ G, float *__restrict__ g,
+                                                      int *__restrict__ err)
+{
+    static_assert(N % 16 == 0 && N >= 16 && N <= 256, "tile shape");
+    constexpr int KD = kWidth;
+    constexpr uint32_t kABytes = kTileM * KD * 2, kDBytes = kTileM * N * 2, kOnesBytes = kTileM * 16 * 2;
+    constexpr uint32_t kCols = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : (2 * N <= 256 ? 256 : 512)));
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *sA = smem;
+    unsigned char *sD = sA + kABytes;
+    unsigned char *sOnes = sD + kDBytes;
+    uint64_t *bar_ld = (uint64_t *)(sOnes + kOnesBytes);
+    uint64_t *bar_mma = bar_ld + 1;
+    uint32_t *tslot = (uint32_t *)(bar_mma + 1);
+    volatile int *sflag = (volatile int *)(tslot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int half = blockIdx.x & 1, split = blockIdx.x >> 1;
+    const int tiles = (M + kTileM - 1) / kTileM;
+    const int t_begin = split * tiles_per_cta;
+    const int t_end = min(tiles, t_begin + tiles_per_cta);
+    const bool with_bias = half == 0 && g != nullptr;
+    for (int i = tid; i < (int)(kOnesBytes / 4); i += blockDim.x)
+        ((uint32_t *)sOnes)[i] = 0x3F803F80u;  // BF16 1.0, 1.0
+    if (warp == 0)
+        tmem_alloc(tslot, kCols);
+    if (tid == 0) {
+        mbar_init(bar_ld, 1);
+        mbar_init(bar_mma, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *sflag = 0;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the ones tile -> tensor core
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t id_main = idesc_bf16_major(kTileM, N, true, true);
+    const uint32_t id_ones = idesc_bf16_major(kTileM, N, false, true);
+    uint32_t ph_ld = 0, ph_mma = 0;
+    int pending = 0;
+    bool failed = false, any = false;
+
+    for (int t = t_begin; t < t_end; ++t) {
+        if (tid == 0) {
+            int st = 0;
+            mbar_expect_tx(bar_ld, kABytes + kDBytes);
+            bulk_g2s(sA, A + (size_t)t * kTileM * KD, kABytes, bar_ld);
+            bulk_g2s(sD, D + (size_t)t * kTileM * N, kDBytes, bar_ld);
+            if (!mbar_wait_bounded(bar_ld, ph_ld)) {
+                st = 1;
+                pending = 1;
+            } else {
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(sA) + (uint32_t)half * 16u * 128u;  // 16 core matrices along MN
+                const uint32_t d0 = smem_u32(sD), o0 = smem_u32(sOnes);
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < RN; ++j)
-            acc[i][j] = 0.0f;
-#pragma unroll
-    for (int j = 0; j < RN; ++j)
-        bacc[j] = 0.0f;
-    for (int m0 = m_begin; m0 < m_end; m0 += RM) {
-        // stage RM rows: A columns [k0, k0+64) and D columns [n0, n0+TN), 8 values per load
-        for (int i = tid; i < RM * (TK / 8); i += 256) {
-            const int mm = i / (TK / 8), c8 = i % (TK / 8);
-            const int m = m0 + mm;
-            __align__(16) bf16 v[8];
-            if (m < m_end && k0 + c8 * 8 < Kd)
-                *(uint4 *)v = *(const uint4 *)(A + tiled_offset(m, k0 + c8 * 8, Kd));
-            else
-                *(uint4 *)v = make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                sa[mm][c8 * 8 + j] = __bfloat162float(v[j]);
+                for (int s = 0; s < kTileM / 16; ++s) {
+                    const uint32_t acc = (t > t_begin || s > 0) ? 1u : 0u;
+                    const uint64_t dd = smem_desc_mn(d0 + (uint32_t)s * 2u * N * 16u, N);
+                    mma_bf16(tmem, smem_desc_mn(a0 + (uint32_t)s * 2u * KD * 16u, KD), dd, id_main, acc);
+                    if (with_bias)
+                        mma_bf16(tmem + (uint32_t)N, smem_desc(o0, 128, 256), dd, id_ones, acc);
+                }
+                mma_commit(bar_mma);
+                if (!mbar_wait_bounded(bar_mma, ph_mma)) {
+                    st = 2;
+                    pending = 2;
+                }
+            }
+            *sflag = st;
         }
-        for (int i = tid; i < RM * (TN / 8); i += 256) {
-            const int mm = i / (TN / 8), c8 = i % (TN / 8);
-            const int m = m0 + mm;
-            __align__(16) bf16 v[8];
-            if (m < m_end && n0 + c8 * 8 < N)
-                *(uint4 *)v = *(const uint4 *)(D + tiled_offset(m, n0 + c8 * 8, N));
-            else
-                *(uint4 *)v = make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                sd[mm][c8 * 8 + j] = __bfloat162float(v[j]);
-        }
+        ph_ld ^= 1u;
+        ph_mma ^= 1u;
         __syncthreads();
-#pragma unroll 8
-        for (int mm = 0; mm < RM; ++mm) {
-            const float4 a = *(const float4 *)&sa[mm][ty * 4];
-            float d[RN];
+        if (*sflag) {
+            failed = true;
+            if (tid == 0 && err)
+                atomicExch(err, 1);
+            break;
+        }
+        any = true;
+    }
+    if (!failed && any) {
+        tc_fence_after();
+        const int k = half * 128 + warp * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tmem_ld16(trow + (uint32_t)c0, v);
+            float4 *dst = (float4 *)(G + (size_t)k * N + c0);
 #pragma unroll
-            for (int j = 0; j < RN; ++j)
-                d[j] = sd[mm][tx * RN + j];
+            for (int q = 0; q < 4; ++q)
+                atomicAdd(dst + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
+        }
+        if (with_bias && warp == 0) {  // every row of the second accumulator holds the column sums
+#pragma unroll 1
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                float v[16];
+                tmem_ld16(trow + (uint32_t)(N + c0), v);
+                if (lane == 0) {
+                    float4 *dst = (float4 *)(g + c0);
 #pragma unroll
-            for (int j = 0; j < RN; ++j) {
-                acc[0][j] += a.x * d[j];
-                acc[1][j] += a.y * d[j];
-                acc[2][j] += a.z * d[j];
-                acc[3][j] += a.w * d[j];
-                bacc[j] += d[j];
+                    for (int q = 0; q < 4; ++q)
+                        atomicAdd(dst + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
+                }
             }
         }
-        __syncthreads();
     }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int k = k0 + ty * 4 + i;
-        if (k >= Kd)
-            continue;
-#pragma unroll
-        for (int j = 0; j < RN; ++j) {
-            const int n = n0 + tx * RN + j;
-            if (n < N)
-                atomicAdd(&G[(size_t)k * N + n], acc[i][j]);
-        }
+    if (failed && tid == 0) {
+        if (pending == 1)
+            mbar_wait_bounded(bar_ld, ph_ld ^ 1u);
+        else if (pending == 2)
+            mbar_wait_bounded(bar_mma, ph_mma ^ 1u);
     }
-    if (g && blockIdx.x == 0 && ty == 0) {
-#pragma unroll
-        for (int j = 0; j < RN; ++j) {
-            const int n = n0 + tx * RN + j;
-            if (n < N)
-                atomicAdd(&g[n], bacc[j]);
-        }
-    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        tmem_dealloc(tmem, kCols);
+}
+
+template <int N>
+void launch_wgrad(const bf16 *A, const bf16 *D, int M, float *G, float *g, int *err, cudaStream_t s)
+{
+    if (M <= 0)
+        return;
+    const size_t smem = (size_t)kTileM * kWidth * 2 + (size_t)kTileM * N * 2 + (size_t)kTileM * 16 * 2 + 64;
+    check_cuda(cudaFuncSetAttribute(k_wgrad_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+               "weight-gradient shared memory");
+    const int tiles = (M + kTileM - 1) / kTileM;
+    const int per = (tiles + 31) / 32;
+    const int splits = (tiles + per - 1) / per;
+    k_wgrad_tc<N><<<2 * splits, 128, smem, s>>>(A, D, M, per, G, g, err);
+    count_launch();
+    check_cuda(cudaGetLastError(), "weight-gradient launch");
 }
 
 // input-layer gradient: G1[k, n] += sum_m x[m, k] D[m, n] (k < 2), g1[n] += sum_m D[m, n];
@@ -589,9 +666,24 @@ __global__ void k_gather_batch(const float *__restrict__ xs, const float *__rest
     }
 }
 
-// head statistics: mean and standard deviation over the H heads
+// inputs of grid points [r0, r0 + rows) of an nx x ny grid (point iy * nx + ix),
+// each coordinate mapped to [-1, 1]
+__global__ void k_grid_inputs(int nx, int ny, long long r0, int rows, float *__restrict__ xb)
+{
+    const float sx = nx > 1 ? 2.0f / (float)(nx - 1) : 0.0f, sy = ny > 1 ? 2.0f / (float)(ny - 1) : 0.0f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+        const long long p = r0 + i;
+        const int ix = (int)(p % nx), iy = (int)(p / nx);
+        xb[2 * i] = nx > 1 ? (float)ix * sx - 1.0f : 0.0f;
+        xb[2 * i + 1] = ny > 1 ? (float)iy * sy - 1.0f : 0.0f;
+    }
+}
+
+// head statistics: mean and standard deviation over the H heads; when
+// `scaled` is given it also receives mean * scale[k] + offset[k]
 __global__ void k_head_stats(const float *__restrict__ out, long long M, int H, int K, float *__restrict__ mean,
-                             float *__restrict__ spread)
+                             float *__restrict__ spread, const float *__restrict__ scale,
+                             const float *__restrict__ offset, float *__restrict__ scaled)
 {
     const long long total = M * K;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
@@ -607,6 +699,8 @@ __global__ void k_head_stats(const float *__restrict__ out, long long M, int H, 
         float mu = s / H;
         mean[idx] = mu;
         spread[idx] = sqrtf(fmaxf(s2 / H - mu * mu, 0.0f));
+        if (scaled)
+            scaled[idx] = mu * (scale ? scale[k] : 1.0f) + (offset ? offset[k] : 0.0f);
     }
 }
 
@@ -728,20 +822,18 @@ int rows_per_block_for(int M, int max_blocks_z)
 }
 }  // namespace
 
-void weight_grad(const bf16 *A, int Kd, const bf16 *D, int N, int M, float *G, float *g, cudaStream_t s)
+void weight_grad(const bf16 *A, const bf16 *D, int N, int M, float *G, float *g, int *err, cudaStream_t s)
 {
-    if (M <= 0)
-        return;
-    const int rpb = rows_per_block_for(M, 8);
-    const unsigned int gz = (unsigned int)((M + rpb - 1) / rpb);
-    if (N % 64 == 0) {
-        dim3 grid((Kd + 63) / 64, N / 64, gz);
-        k_weight_grad<64><<<grid, 256, 0, s>>>(A, Kd, D, N, M, rpb, G, g);
-    } else {
-        dim3 grid((Kd + 63) / 64, (N + 15) / 16, gz);
-        k_weight_grad<16><<<grid, 256, 0, s>>>(A, Kd, D, N, M, rpb, G, g);
-    }
-    after_launch("weight gradient launch");
+    if (N == 256)
+        launch_wgrad<256>(A, D, M, G, g, err, s);
+    else if (N == 64)
+        launch_wgrad<64>(A, D, M, G, g, err, s);
+    else if (N == 32)
+        launch_wgrad<32>(A, D, M, G, g, err, s);
+    else if (N == 16)
+        launch_wgrad<16>(A, D, M, G, g, err, s);
+    else
+        fail(CLODE_ERR_INVALID_ARGUMENT, "weight gradient: N must be 16, 32, 64 or 256 (got %d)", N);
 }
 
 void weight_grad_input(const float *x, const bf16 *D, int M, float *G, float *g, cudaStream_t s)
@@ -778,10 +870,17 @@ void gather_batch(const float *xs, const float *ys, int n_rows, int K, int B, co
     after_launch("batch gather launch");
 }
 
-void head_stats(const float *out, long long M, int H, int K, float *mean, float *spread, cudaStream_t s)
+void head_stats(const float *out, long long M, int H, int K, float *mean, float *spread, cudaStream_t s,
+                const float *scale, const float *offset, float *scaled)
 {
-    k_head_stats<<<grid_for((size_t)M * K), kThreads, 0, s>>>(out, M, H, K, mean, spread);
+    k_head_stats<<<grid_for((size_t)M * K), kThreads, 0, s>>>(out, M, H, K, mean, spread, scale, offset, scaled);
     after_launch("head statistics launch");
+}
+
+void grid_inputs(int nx, int ny, long long r0, int rows, float *xb, cudaStream_t s)
+{
+    k_grid_inputs<<<grid_for((size_t)rows), kThreads, 0, s>>>(nx, ny, r0, rows, xb);
+    after_launch("grid inputs launch");
 }
 
 void screen_grid(const float *mean, const float *spread, int nx, int ny, int K, const float *spread_thr,

@@ -53,8 +53,10 @@ void linear_back_heads(const bf16 *dZ, int M, const bf16 *Wbwd, const bf16 *mask
 // h1 = sin(x W1 + b1), c1 = cos(x W1 + b1)  (tiled BF16, width 256)
 void input_layer(const float *x, int M, const float *W1, const float *b1, bf16 *h1, bf16 *c1, cudaStream_t s);
 void mse(const float *out, const float *y, int M, int H, int K, bf16 *dz, float *loss, cudaStream_t s);
-// G += A^T D, g += column sums of D  (A, D tiled BF16; G, g zeroed by the caller)
-void weight_grad(const bf16 *A, int Kd, const bf16 *D, int N, int M, float *G, float *g, cudaStream_t s);
+// G += A^T D, g += column sums of D on the tensor cores (A: tiled BF16 width
+// 256, D: tiled BF16 width N in {16, 32, 64, 256}, zero rows past M; G, g
+// 16-byte aligned, zeroed by the caller)
+void weight_grad(const bf16 *A, const bf16 *D, int N, int M, float *G, float *g, int *err, cudaStream_t s);
 // G1 += x^T D, g1 += column sums of D  (x FP32 [M x 2], D tiled BF16 width 256)
 void weight_grad_input(const float *x, const bf16 *D, int M, float *G, float *g, cudaStream_t s);
 void adam_all(float *w, const float *grad, float *m1, float *m2, size_t n, float lr, const int *step,
@@ -63,7 +65,9 @@ void adam_all(float *w, const float *grad, float *m1, float *m2, size_t n, float
 void write_images(const float *w, const WeightImages *img, int n_img, cudaStream_t s);
 void gather_batch(const float *xs, const float *ys, int n_rows, int K, int B, const int *cursor, float *xb, float *yb,
                   int *step, float *loss, cudaStream_t s);
-void head_stats(const float *out, long long M, int H, int K, float *mean, float *spread, cudaStream_t s);
+void head_stats(const float *out, long long M, int H, int K, float *mean, float *spread, cudaStream_t s,
+                const float *scale = nullptr, const float *offset = nullptr, float *scaled = nullptr);
+void grid_inputs(int nx, int ny, long long r0, int rows, float *xb, cudaStream_t s);
 void screen_grid(const float *mean, const float *spread, int nx, int ny, int K, const float *spread_thr,
                  const float *jump_thr, int *flags, cudaStream_t s);
 

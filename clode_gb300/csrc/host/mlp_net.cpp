@@ -1,7 +1,7 @@
 // The surrogate network object behind the clode_mlp_* entry points: FP32
 // master parameters with Adam moments, BF16 images of the tensor-core layer
 // weights in both operand orders, the training data resident on the device,
-// and one training step (13 kernels and a memset) captured as a CUDA graph
+// and one training step (14 kernels and a memset) captured as a CUDA graph
 // and replayed.
 //
 // Parameter vector layout (FP32, row-major [in x out]):
@@ -74,7 +74,7 @@ struct clode_mlp {
     Buf xs, ys, counters, loss_hist;  // counters: [0] step, [1] cursor, [2] error flag, [3] loss, [4] history index
     long long data_rows = 0;
     // prediction results
-    Buf pred_mean, pred_spread;
+    Buf pred_mean, pred_spread, pred_scaled;
     long long pred_rows = 0;
     Buf thr, flags;
     double train_ms = 0, predict_ms = 0;
@@ -97,7 +97,7 @@ struct clode_mlp {
         if (graph)
             cudaGraphExecDestroy(graph);
         for (Buf *b : {&params, &grads, &m1, &m2, &wf2, &wb2, &wf3, &wb3, &wfh, &wbh, &xb, &yb, &h1, &c1, &h2, &h3,
-                       &out, &dzo, &dz3, &dz2, &dz1, &xs, &ys, &counters, &loss_hist, &pred_mean, &pred_spread, &thr,
+                       &out, &dzo, &dz3, &dz2, &dz1, &xs, &ys, &counters, &loss_hist, &pred_mean, &pred_spread, &pred_scaled, &thr,
                        &flags})
             b->release();
         if (stream)
@@ -211,13 +211,13 @@ struct clode_mlp {
     {
         check_cuda(cudaMemsetAsync(grads.p, 0, n_params * 4, stream), "gradient reset");
         mlp::mse(out.as<float>(), yb.as<float>(), rows, H, K, dzo.as<bf16>(), loss_acc(), stream);
-        mlp::weight_grad(h3.as<bf16>(), kWidth, dzo.as<bf16>(), HK, rows, G(oWh), G(obh), stream);
+        mlp::weight_grad(h3.as<bf16>(), dzo.as<bf16>(), HK, rows, G(oWh), G(obh), err_flag(), stream);
         mlp::linear_back_heads(dzo.as<bf16>(), rows, wbh.as<bf16>(), h3.as<bf16>(), dz3.as<bf16>(), HK, err_flag(),
                                sms, stream);
-        mlp::weight_grad(h2.as<bf16>(), kWidth, dz3.as<bf16>(), kWidth, rows, G(oW3), G(ob3), stream);
+        mlp::weight_grad(h2.as<bf16>(), dz3.as<bf16>(), kWidth, rows, G(oW3), G(ob3), err_flag(), stream);
         mlp::linear_back_relu(dz3.as<bf16>(), rows, wb3.as<bf16>(), h2.as<bf16>(), dz2.as<bf16>(), err_flag(), sms,
                               stream);
-        mlp::weight_grad(h1.as<bf16>(), kWidth, dz2.as<bf16>(), kWidth, rows, G(oW2), G(ob2), stream);
+        mlp::weight_grad(h1.as<bf16>(), dz2.as<bf16>(), kWidth, rows, G(oW2), G(ob2), err_flag(), stream);
         mlp::linear_back_mul(dz2.as<bf16>(), rows, wb2.as<bf16>(), c1.as<bf16>(), dz1.as<bf16>(), err_flag(), sms,
                              stream);
         mlp::weight_grad_input(xb.as<float>(), dz1.as<bf16>(), rows, G(oW1), G(ob1), stream);
@@ -355,6 +355,38 @@ struct clode_mlp {
         check_error_flag();
     }
 
+    void predict_grid(int nx, int ny, const float *out_scale, const float *out_offset, float *out_h)
+    {
+        use_device(device);
+        const long long n = (long long)nx * ny;
+        const int chunk = 1 << 22;
+        ensure_capacity((int)std::min<long long>(n, chunk));
+        pred_mean.reserve((size_t)std::max<long long>(n, 1) * K * 4);
+        pred_spread.reserve((size_t)std::max<long long>(n, 1) * K * 4);
+        pred_scaled.reserve((size_t)std::max<long long>(n, 1) * K * 4);
+        thr.reserve((size_t)2 * K * 4);
+        std::vector<float> so(2 * (size_t)K);
+        for (int k = 0; k < K; ++k) {
+            so[k] = out_scale ? out_scale[k] : 1.0f;
+            so[K + k] = out_offset ? out_offset[k] : 0.0f;
+        }
+        pred_rows = n;
+        auto t0 = std::chrono::steady_clock::now();
+        check_cuda(cudaMemcpyAsync(thr.p, so.data(), so.size() * 4, cudaMemcpyHostToDevice, stream), "H2D");
+        for (long long r0 = 0; r0 < n; r0 += chunk) {
+            int rows = (int)std::min<long long>(chunk, n - r0);
+            mlp::grid_inputs(nx, ny, r0, rows, xb.as<float>(), stream);
+            forward(rows);
+            mlp::head_stats(out.as<float>(), rows, H, K, pred_mean.as<float>() + r0 * K,
+                            pred_spread.as<float>() + r0 * K, stream, thr.as<float>(), thr.as<float>() + K,
+                            pred_scaled.as<float>() + r0 * K);
+        }
+        check_cuda(cudaMemcpyAsync(out_h, pred_scaled.p, (size_t)n * K * 4, cudaMemcpyDeviceToHost, stream), "D2H");
+        check_cuda(cudaStreamSynchronize(stream), "grid prediction");
+        predict_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        check_error_flag();
+    }
+
     void screen(int nx, int ny, const float *spread_thr, const float *jump_thr, int *flags_out)
     {
         if ((long long)nx * ny != pred_rows)
@@ -466,6 +498,16 @@ int clode_mlp_predict(clode_mlp *net, const float *x, long long n, float *mean, 
         if (!net || !x || n < 0)
             fail(CLODE_ERR_INVALID_ARGUMENT, "invalid arguments");
         net->predict(x, n, mean, spread, heads);
+    });
+}
+
+int clode_mlp_predict_grid(clode_mlp *net, int nx, int ny, const float *out_scale, const float *out_offset,
+                           float *out)
+{
+    return mlp_guard([&] {
+        if (!net || !out || nx < 1 || ny < 1)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "invalid arguments");
+        net->predict_grid(nx, ny, out_scale, out_offset, out);
     });
 }
 

@@ -96,6 +96,16 @@ class MLP:
         _check(N.lib.clode_mlp_predict(self._h, _fp(x), n, _fp(mean), _fp(spread), _fp(hv)))
         return (mean, spread, hv) if heads else (mean, spread)
 
+    def predict_grid(self, nx: int, ny: int, scale=None, offset=None) -> np.ndarray:
+        """Mean over the heads on the nx x ny grid of inputs in [-1, 1]^2
+        (point iy * nx + ix), generated on the device; returns
+        mean * scale + offset as float32, shape (nx * ny, K)."""
+        out = np.empty((nx * ny, self.K), dtype=np.float32)
+        sc = None if scale is None else np.ascontiguousarray(scale, dtype=np.float32)
+        of = None if offset is None else np.ascontiguousarray(offset, dtype=np.float32)
+        _check(N.lib.clode_mlp_predict_grid(self._h, nx, ny, _fp(sc), _fp(of), _fp(out)))
+        return out
+
     def screen(self, nx: int, ny: int, spread_thr, jump_thr) -> np.ndarray:
         """Flags of the last prediction on an nx x ny grid: 1 = heads disagree, 2 = neighbour jump."""
         st = np.ascontiguousarray(spread_thr, dtype=np.float32)
@@ -171,26 +181,38 @@ class FeatureMapScreen:
     def _calibrate(r, v, err, tol, keep):
         """Thresholds (r_max, v_max) on the sample's cell statistics such that
         at least `keep` of the accepted sample points have err <= tol; the pair
-        accepting the most points.  Returns (r_max, v_max, accepted fraction),
-        (-1, -1, 0) when no pair qualifies."""
-        qs = np.concatenate([np.linspace(0.0, 0.95, 39), [0.975, 0.99, 1.0]])
+        accepting the most points.  r_max runs over every sample value (prefix
+        sums in r order), v_max over quantiles of v.  Returns (r_max, v_max,
+        accepted fraction), (-1, -1, 0) when no pair qualifies."""
+        n = r.size
         best = (-1.0, -1.0, 0.0)
+        if n == 0:
+            return best
         good = err <= tol
-        for tr in np.unique(np.quantile(r, qs)):
-            ok_r = r <= tr
-            for tv in np.unique(np.quantile(v, qs)):
-                acc = ok_r & (v <= tv)
-                frac = float(acc.mean())
-                if frac <= best[2] or not acc.any():
-                    continue
-                if good[acc].mean() >= keep:
-                    best = (float(tr), float(tv), frac)
+        order = np.argsort(r, kind="stable")
+        r_s, v_s, g_s = r[order], v[order], good[order]
+        last_of_tie = np.r_[r_s[1:] != r_s[:-1], True]
+        qs = np.concatenate([np.linspace(0.0, 0.95, 39), [0.975, 0.99, 1.0]])
+        for tv in np.unique(np.quantile(v, qs)):
+            m = v_s <= tv
+            acc = np.cumsum(m)
+            ok = np.cumsum(m & g_s)
+            valid = last_of_tie & (acc > 0) & (ok >= keep * acc)
+            if not valid.any():
+                continue
+            idx = np.nonzero(valid)[0]
+            j = idx[np.argmax(acc[idx])]
+            frac = float(acc[j]) / n
+            if frac > best[2]:
+                best = (float(r_s[j]), float(tv), frac)
         return best
 
     def run(self, nx: int, ny: int, train_stride: int = 8, steps: int = 3000, batch: int = 4096,
             lr: float = 2e-3, tol: float = 0.01, keep: float = 0.99, n_calibration: int = 65536) -> ScreenResult:
-        """Screened map of the nx x ny grid (point m = iy * nx + ix)."""
+        """Screened map of the nx x ny grid (point m = iy * nx + ix); features
+        are float32 (the FP32 engine's values are exact in float32)."""
         t_all = time.perf_counter()
+        K = self.K
         g0 = np.linspace(self.lo[0], self.hi[0], nx)
         g1 = np.linspace(self.lo[1], self.hi[1], ny)
         # 1. the sub-grid (every train_stride-th line and the last one) integrated by the engine
@@ -212,26 +234,24 @@ class FeatureMapScreen:
                   for ph in range(4)]
         loss = np.concatenate(losses)
         t_train = time.perf_counter() - t0
-        # 3. prediction of the full grid
+        # 3. prediction of the full grid (inputs generated and outputs rescaled on the device)
         t0 = time.perf_counter()
-        PX, PY = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
-        mean, _ = self.net.predict(self._norm_x(g0[PX.ravel()], g1[PY.ravel()]))
-        F = mean.astype(np.float64) * sd + mu
+        F = self.net.predict_grid(nx, ny, sd, mu)
         t_predict = time.perf_counter() - t0
         # 4. cell statistics from the integrated corners
         t0 = time.perf_counter()
-        Fs = Fsub.reshape(sy.size, sx.size, self.K)
-        Ps = F.reshape(ny, nx, self.K)[np.ix_(sy, sx)]
+        Fs = Fsub.reshape(sy.size, sx.size, K)
+        Ps = F.reshape(ny, nx, K)[np.ix_(sy, sx)].astype(np.float64)
         R = (np.abs(Ps - Fs) / scale).max(axis=2)
-        r_cell = np.maximum.reduce([R[:-1, :-1], R[:-1, 1:], R[1:, :-1], R[1:, 1:]]) if R.shape[0] > 1 and R.shape[1] > 1 \
-            else np.zeros((0, 0))
-        cmax = np.maximum.reduce([Fs[:-1, :-1], Fs[:-1, 1:], Fs[1:, :-1], Fs[1:, 1:]])
-        cmin = np.minimum.reduce([Fs[:-1, :-1], Fs[:-1, 1:], Fs[1:, :-1], Fs[1:, 1:]])
-        v_cell = ((cmax - cmin) / scale).max(axis=2)
-        cx = np.clip(np.searchsorted(sx, np.arange(nx), side="right") - 1, 0, sx.size - 2)
-        cy = np.clip(np.searchsorted(sy, np.arange(ny), side="right") - 1, 0, sy.size - 2)
-        r_pt = r_cell[cy[:, None], cx[None, :]].ravel()
-        v_pt = v_cell[cy[:, None], cx[None, :]].ravel()
+        corners = lambda A: (A[:-1, :-1], A[:-1, 1:], A[1:, :-1], A[1:, 1:])
+        if sx.size > 1 and sy.size > 1:
+            r_cell = np.maximum.reduce(corners(R))
+            v_cell = ((np.maximum.reduce(corners(Fs)) - np.minimum.reduce(corners(Fs))) / scale).max(axis=2)
+        else:  # a single grid line: no cells, everything is integrated
+            r_cell = np.full((1, 1), np.inf)
+            v_cell = np.full((1, 1), np.inf)
+        cx = np.clip(np.searchsorted(sx, np.arange(nx), side="right") - 1, 0, r_cell.shape[1] - 1)
+        cy = np.clip(np.searchsorted(sy, np.arange(ny), side="right") - 1, 0, r_cell.shape[0] - 1)
         flags = np.full(nx * ny, ScreenResult.SURROGATE, dtype=np.int8)
         flags[sub] = ScreenResult.SAMPLED
         F[sub] = Fsub
@@ -239,19 +259,28 @@ class FeatureMapScreen:
         # 5. calibration sample: random interior points, integrated exactly
         t0 = time.perf_counter()
         rng = np.random.default_rng(self.seed + 101)
-        interior = np.nonzero(flags == ScreenResult.SURROGATE)[0]
-        cal = rng.choice(interior, size=min(n_calibration, interior.size), replace=False) if interior.size else \
-            np.zeros(0, dtype=np.int64)
-        Fcal = np.asarray(self.integrate(g0[cal % nx], g1[cal // nx]), dtype=np.float64) if cal.size else \
-            np.zeros((0, self.K))
-        tr, tv, acc = self._calibrate(r_pt[cal], v_pt[cal], self.map_error(F[cal], Fcal, scale), tol, keep) \
-            if cal.size else (-1.0, -1.0, 0.0)
-        F[cal] = Fcal
-        flags[cal] = ScreenResult.SAMPLED
+        n_int = nx * ny - sub.size
+        want = min(n_calibration, n_int)
+        cal = np.zeros(0, dtype=np.int64)
+        while cal.size < want:
+            cand = rng.integers(0, nx * ny, size=2 * (want - cal.size) + 16)
+            cand = cand[flags[cand] == ScreenResult.SURROGATE]
+            cal = np.unique(np.r_[cal, cand])
+        if cal.size > want:
+            cal = rng.choice(cal, size=want, replace=False)
+        tr, tv, acc = -1.0, -1.0, 0.0
+        if cal.size:
+            ix, iy = cal % nx, cal // nx
+            Fcal = np.asarray(self.integrate(g0[ix], g1[iy]), dtype=np.float64)
+            err_cal = self.map_error(F[cal], Fcal, scale)
+            tr, tv, acc = self._calibrate(r_cell[cy[iy], cx[ix]], v_cell[cy[iy], cx[ix]], err_cal, tol, keep)
+            F[cal] = Fcal
+            flags[cal] = ScreenResult.SAMPLED
         t_cal = time.perf_counter() - t0
         # 6. fallback: the plain engine on every point of a rejected cell
         t0 = time.perf_counter()
-        reject = (flags == ScreenResult.SURROGATE) & ((r_pt > tr) | (v_pt > tv))
+        reject_cell = (r_cell > tr) | (v_cell > tv)
+        reject = reject_cell[cy[:, None], cx[None, :]].ravel() & (flags == ScreenResult.SURROGATE)
         redo = np.nonzero(reject)[0]
         if redo.size:
             F[redo] = np.asarray(self.integrate(g0[redo % nx], g1[redo // nx]), dtype=np.float64)
@@ -263,4 +292,5 @@ class FeatureMapScreen:
             "calibrate_s": t_cal, "fallback_s": t_fallback, "total_s": total, "points": nx * ny,
             "points_per_s": nx * ny / total, "training_points": int(sub.size), "calibration_points": int(cal.size),
             "fallback_points": int(redo.size), "integrated_points": int(np.count_nonzero(flags)),
-            "r_max": tr, "v_max": tv, "calibrated_accept_fraction": acc, "feature_scale": scale.tolist()})
+            "r_max": tr, "v_max": tv, "calibrated_accept_fraction": acc, "rejected_cells": int(reject_cell.sum()),
+            "cells": int(reject_cell.size), "feature_scale": scale.tolist()})

@@ -307,6 +307,13 @@ int clode_mlp_train(clode_mlp *net, const float *x, const float *y, long long n,
                     unsigned long long seed, float *loss_history);
 /* mean and standard deviation over the heads, [n x n_outputs] each; heads [n x H*K] may be NULL */
 int clode_mlp_predict(clode_mlp *net, const float *x, long long n, float *mean, float *spread, float *heads);
+/* mean over the heads at every point of an nx x ny grid of inputs
+ * x = (-1 + 2 ix / (nx - 1), -1 + 2 iy / (ny - 1)) (0 when the extent is 1),
+ * point iy * nx + ix, generated on the device; out[p * K + k] =
+ * mean * out_scale[k] + out_offset[k] (scale/offset may be NULL: 1 / 0).
+ * The prediction is kept for clode_mlp_screen. */
+int clode_mlp_predict_grid(clode_mlp *net, int nx, int ny, const float *out_scale, const float *out_offset,
+                           float *out);
 /* flags of the last prediction laid out as an nx x ny grid (point iy*nx + ix):
  * bit 0 = head spread above spread_thr[k], bit 1 = jump to a 4-neighbour above jump_thr[k] */
 int clode_mlp_screen(clode_mlp *net, int nx, int ny, const float *spread_thr, const float *jump_thr, int *flags);

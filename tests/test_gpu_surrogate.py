@@ -50,6 +50,23 @@ def test_gradients_match_oracle():
         assert err < 2e-2, (name, err)
 
 
+def test_grid_prediction_matches_point_prediction():
+    net = _net(seed=11)
+    nx, ny = 300, 211  # not multiples of the 128-row tile
+    gx = np.linspace(-1, 1, nx, dtype=np.float64)
+    gy = np.linspace(-1, 1, ny, dtype=np.float64)
+    X0, X1 = np.meshgrid(gx, gy, indexing="xy")
+    x = np.stack([X0.ravel(), X1.ravel()], axis=1).astype(np.float32)
+    mean, _ = net.predict(x)
+    scale = np.array([2.0, -1.0, 0.5, 3.0], dtype=np.float32)
+    offset = np.array([0.0, 1.0, -2.0, 0.25], dtype=np.float32)
+    grid = net.predict_grid(nx, ny, scale, offset)
+    # tolerance: the device computes the grid coordinates in FP32, the host in
+    # float64 rounded once; an ulp of input moves the sine layer slightly
+    np.testing.assert_allclose(grid, mean * scale + offset, rtol=0, atol=2e-2 * np.abs(mean).max() * 3.0)
+    assert np.median(np.abs(grid - (mean * scale + offset))) < 1e-3 * np.abs(mean).max() * 3.0
+
+
 def test_training_fits_a_smooth_map():
     net = _net(seed=7)
     rng = np.random.default_rng(2)
