@@ -195,14 +195,16 @@ def bench_surrogate(args, tuned_options: dict) -> dict:
     plain = integrate(P0, P1)
     t_plain = time.perf_counter() - t0
     scr = FeatureMapScreen(integrate, lo=(0.5, 0.0), hi=(3.0, 2.0), n_features=len(SURROGATE_FEATURES), seed=1)
-    res = scr.run(G, G, train_stride=max(G // 512, 1), steps=args.surrogate_steps, batch=4096, tol=0.01,
-                  keep=0.99, n_calibration=65536)
+    res = scr.run(G, G, train_stride=max(G // 512, 1), steps=args.surrogate_steps, batch=args.surrogate_batch,
+                  tol=0.01, keep=0.99, n_calibration=65536, refine=bool(args.surrogate_refine))
     scale = plain.max(axis=0) - plain.min(axis=0)
     err = FeatureMapScreen.map_error(res.features, plain, scale)
     rng = np.random.default_rng(args.seed ^ 0xC0DE)
     held = rng.choice(G * G, size=min(65536, G * G), replace=False)
     return {
         "workload": f"lactotroph nhood2 map {G}x{G}, tspan [0,3000] ms, features {list(SURROGATE_FEATURES)}",
+        "training": {"steps": args.surrogate_steps, "batch": args.surrogate_batch,
+                     "refine": bool(args.surrogate_refine)},
         "error_measure": "max over features of |screened - plain| / feature range over the plain map",
         "points": G * G, "plain_points_per_s": G * G / t_plain, "screened_points_per_s": res.timings["points_per_s"],
         "speedup_vs_plain": t_plain / res.timings["total_s"], "integrated_fraction": res.integrated_fraction,
@@ -216,6 +218,56 @@ def bench_surrogate(args, tuned_options: dict) -> dict:
                       if k != "feature_scale"},
         "plain_s": t_plain,
     }
+
+
+def bench_trajectory(args, tuned_options: dict) -> dict:
+    """Stored trajectories of the Ornstein-Uhlenbeck process (the reference's
+    stochastic example): theta = linspace(0.1, 2, 16) x sigma = linspace(0.1,
+    1, 16) parameter points x 256 realisations = 65,536 members, x0 = 0,
+    mu = 0, seeded RNG, stochastic Euler dt = 1e-3 over [0, 100] (100,000
+    steps), a row (t, x, dx) stored every 10 steps: 10,001 rows, 7.87 GB
+    written in FP32.  Reports member-steps/s and the write bandwidth of the
+    trajectory launch against the measured HBM copy bandwidth."""
+    from clode_gb300 import clode_cpp_wrapper as W, rhs_path
+
+    pi = W.ProblemInfo(rhs_path("ornstein_uhlenbeck.cl"), ["x"], ["theta", "mu", "sigma"], [], 1)
+    sim = W.TrajectorySimulatorBase(pi, "seuler", True, W.OpenCLResource(), "")
+    for k in ("schedule", "block_size", "fmad", "prec_div", "ftz"):
+        if k in tuned_options:
+            sim.set_option(k, tuned_options[k])
+    sim.build_cl()
+    steps, nout = args.trajectory_steps, 10
+    sim.set_solver_params(W.SolverParams(dt=1e-3, dtmax=1.0, abstol=1e-6, reltol=1e-3, max_steps=steps,
+                                         max_store=steps // nout + 2, nout=nout))
+    th, sg = np.meshgrid(np.linspace(0.1, 2.0, 16), np.linspace(0.1, 1.0, 16), indexing="xy")
+    pts = np.stack([th.ravel(), np.zeros(256), sg.ravel()], axis=1)
+    pars = np.repeat(pts, 256, axis=0)
+    n = pars.shape[0]
+    sim.set_problem_data(np.zeros(n), pars.flatten(order="F"))
+    sim.set_tspan([0.0, steps * 1e-3])
+    times = []
+    for rep in range(3):
+        sim.seed_rng(args.seed + rep)
+        sim.trajectory()
+        times.append(sim.last_kernel_ms())
+    rows = int(np.asarray(sim.get_n_stored()).max()) + 1
+    ms = float(min(times))
+    written = rows * n * 3 * 4
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    gbs = written / (ms / 1e3) / 1e9
+    return {"workload": f"OU trajectories, 65536 members (256 parameter points x 256 realisations), seuler "
+                        f"dt 1e-3 over [0, {steps * 1e-3:g}], (t, x, dx) stored every 10 steps, FP32",
+            "members": n, "steps_per_member": steps, "rows": rows, "ms": ms, "ms_all": times,
+            "member_steps_per_s": n * steps / (ms / 1e3),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                         "traffic": None, "algorithmic_bytes": written,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"}}
 
 
 def bench_reference_arm(args):
@@ -268,7 +320,11 @@ def main():
     ap.add_argument("--autotune", type=int, default=262144, help="autotune on this many members first (0: off)")
     ap.add_argument("--surrogate-grid", type=int, default=4096)
     ap.add_argument("--surrogate-steps", type=int, default=3000)
+    ap.add_argument("--surrogate-batch", type=int, default=4096)
+    ap.add_argument("--surrogate-refine", type=int, default=0)
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-trajectory", action="store_true")
+    ap.add_argument("--trajectory-steps", type=int, default=100000)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
 
@@ -433,13 +489,18 @@ def main():
                                 "event_count_exact_frac": float(np.mean(Fg[:, ev] == Fc[:, ev])),
                                 "mean_period_rel_err_median": float(np.median(rel)),
                                 "mean_period_rel_err_p99": float(np.quantile(rel, 0.99))}
-    if rank == 0 and not args.no_surrogate:
-        opts = {k: sim.get_option(k) for k in ("schedule", "block_size", "maxrregcount", "fmad", "prec_div", "ftz",
+    opts = {k: sim.get_option(k) for k in ("schedule", "block_size", "maxrregcount", "fmad", "prec_div", "ftz",
                                            "fast_math")}
+    if rank == 0 and not args.no_surrogate:
         try:
             line["surrogate"] = bench_surrogate(args, opts)
         except Exception as e:  # reported, not hidden: the plain line stands on its own
             line["surrogate"] = {"error": f"{type(e).__name__}: {e}"}
+    if rank == 0 and not args.no_trajectory:
+        try:
+            line["trajectory"] = bench_trajectory(args, opts)
+        except Exception as e:
+            line["trajectory"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

@@ -636,12 +636,16 @@ class SimulatorBase:
         _check(N.lib.clode_sim_chain(self._handle, codes, len(ops), int(bool(use_graph))))
 
     def autotune(self, sample: int = 0) -> dict:
-        """Pick register cap and block size by timing the persistent kernel on
-        members [0, sample) (no reference counterpart)."""
+        """Pick register cap, block size, (adaptive steppers) the stepping
+        variant and (two-pass observers) fused or separate observer
+        initialisation by timing the persistent kernels on members [0, sample)
+        (no reference counterpart)."""
         ms = C.c_double(0.0)
         _check(N.lib.clode_sim_autotune(self._handle, int(sample), C.byref(ms)))
         return {"ms": ms.value, "maxrregcount": int(self.get_option("maxrregcount")),
-                "block_size": int(self.get_option("block_size"))}
+                "block_size": int(self.get_option("block_size")),
+                "split_attempts": int(self.get_option("split_attempts")),
+                "fuse_init": int(self.get_option("fuse_init"))}
 
     def kernel_registers(self, kernel: str) -> int:
         r, t = C.c_int(0), C.c_int(0)

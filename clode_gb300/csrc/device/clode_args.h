@@ -61,6 +61,7 @@ struct ArgsT {
     int nPts;
     int i_begin;
     int i_end;
+    int i_stride;              // persistent kernels: members i_begin, i_begin + i_stride, ... below i_end (<= 1: all)
     int fused_init;            // features: run the observer initialisation in the same launch
     // time span: global [t0, t1] or, when tspan_pm != 0, per member [2*i], [2*i+1]
     R t0;

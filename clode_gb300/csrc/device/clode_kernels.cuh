@@ -131,10 +131,11 @@ __device__ __forceinline__ void flush_counters(const Args &a, const Counters &c)
 }
 
 // ------------------------------------------------------------ scheduling --
-// Persistent schedule: hand out the next members of [i_begin, i_end) to the
-// lanes of this warp that ask for one, with a single atomic per warp.  Every
-// lane of the warp must call it (full-mask vote); lanes with want == false
-// get -1.  Returns -1 as well once the range is exhausted.
+// Persistent schedule: hand out the next members of [i_begin, i_end) (every
+// i_stride-th one when i_stride > 1, as the autotuner samples) to the lanes of
+// this warp that ask for one, with a single atomic per warp.  Every lane of
+// the warp must call it (full-mask vote); lanes with want == false get -1.
+// Returns -1 as well once the range is exhausted.
 __device__ __forceinline__ int fetch_member(const Args &a, bool want)
 {
     const unsigned int lane = threadIdx.x & 31u;
@@ -148,7 +149,8 @@ __device__ __forceinline__ int fetch_member(const Args &a, bool want)
     base = __shfl_sync(0xffffffffu, base, leader);
     if (!want)
         return -1;
-    long long k = (long long)a.i_begin + base + __popc(mask & ((1u << lane) - 1u));
+    const long long stride = a.i_stride > 1 ? a.i_stride : 1;
+    long long k = (long long)a.i_begin + ((long long)base + __popc(mask & ((1u << lane) - 1u))) * stride;
     return k < a.i_end ? (int)k : -1;
 }
 
@@ -195,6 +197,8 @@ extern "C" __global__ void clode_transient_persistent(const Args a)
     bool hmin_fail = false;
     realtype t1 = ZERO;
     Member m;
+    StepCtl sc;
+    sc.retry = false;
     for (;;) {
         bool want = i < 0 && !exhausted;
         if (want && budget_spent(a, t_start)) {
@@ -217,9 +221,10 @@ extern "C" __global__ void clode_transient_persistent(const Args a)
             break;
         if (i < 0)
             continue;
-        if (m.t <= t1 && step < a.sp.max_steps) {
-            ++step;
-            hmin_fail |= step_member(m, a.sp, t1, c) != 0;
+        if (sc.retry || (m.t <= t1 && step < a.sp.max_steps)) {
+            if (!sc.retry)
+                ++step;
+            hmin_fail |= step_attempt(m, a.sp, t1, c, sc) == -1;
         } else {
             member_store(m, a, i);
             if (a.status)
@@ -290,6 +295,8 @@ extern "C" __global__ void clode_trajectory_persistent(const Args a)
     bool hmin_fail = false;
     realtype t1 = ZERO;
     Member m;
+    StepCtl sc;
+    sc.retry = false;
     for (;;) {
         bool want = i < 0 && !exhausted;
         if (want && budget_spent(a, t_start)) {
@@ -314,10 +321,12 @@ extern "C" __global__ void clode_trajectory_persistent(const Args a)
             break;
         if (i < 0)
             continue;
-        if (m.t <= t1 && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store) {
-            ++step;
-            hmin_fail |= step_member(m, a.sp, t1, c) != 0;
-            if (step % a.sp.nout == 0) {
+        if (sc.retry || (m.t <= t1 && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store)) {
+            if (!sc.retry)
+                ++step;
+            const int flag = step_attempt(m, a.sp, t1, c, sc);
+            hmin_fail |= flag == -1;
+            if (flag != 1 && step % a.sp.nout == 0) {
                 ++row;
                 store_row(a, m, i, row);
             }
@@ -396,6 +405,66 @@ extern "C" __global__ void clode_init_observer(const Args a)
     flush_counters(a, c);
 }
 
+// Observer initialisation, persistent schedule: lanes refill themselves, and
+// every lane runs the same (warm-up) pass, so the observer code never
+// diverges between passes.  Not subject to the time budget: every member's
+// observer is initialised.
+extern "C" __global__ void clode_init_observer_persistent(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    bool exhausted = false;
+    int i = -1;
+    bool fresh = false;
+    unsigned int step = 0;
+    realtype t1 = ZERO;
+    Member m;
+    Observer o;
+    StepCtl sc;
+    sc.retry = false;
+    for (;;) {
+        const bool want = i < 0 && !exhausted;
+        const int got = fetch_member(a, want);
+        if (want) {
+            if (got < 0) {
+                exhausted = true;
+            } else {
+                i = got;
+                fresh = true;
+            }
+        }
+        if (__all_sync(0xffffffffu, i < 0))
+            break;
+        if (i < 0)
+            continue;
+        if (fresh) {
+            member_load(m, a, i, c);
+            o.init(m.t, m.x, m.dx, m.aux, a.op);
+            step = 0;
+            t1 = member_t1(a, i);
+            fresh = false;
+        }
+        const bool running = Observer::two_pass && (sc.retry || (step < a.sp.max_steps && m.t < t1));
+        if (running) {
+            if (!sc.retry)
+                ++step;
+            if (step_attempt(m, a.sp, t1, c, sc) != 1)
+                o.warmup(m.t, m.x, m.dx, m.aux, a.op);
+        } else {
+            if (Observer::two_pass) {
+                // rewind to the initial state (the last noise sample is kept)
+                m.t = member_t0(a, i);
+                load_x0(m.x, a, i);
+                getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
+                c.rhs += 1;
+            }
+            o.arm(m.t, m.x, m.dx, m.aux, a.op);
+            park_store(o, a, i);
+            i = -1;
+        }
+    }
+    flush_counters(a, c);
+}
+
 // Feature pass for one member (features.cl:10-106)
 __device__ __forceinline__ void features_member(Observer &o, const Args &a, int i, Counters &c)
 {
@@ -444,8 +513,10 @@ extern "C" __global__ void clode_features(const Args a)
 // Features, persistent schedule.  A lane walks its member through the
 // observer's warm-up pass (two-pass observers, when the initialisation is
 // fused into this launch) and the feature pass, then takes the next member.
-// Both passes go through the same step_member call, so lanes in different
-// passes stay converged on the expensive part of the loop.
+// Both passes go through the same step_attempt call, so lanes in different
+// passes stay converged on the expensive part of the loop, and a rejected
+// adaptive attempt is retried in the next iteration instead of holding the
+// warp for a repeat.
 extern "C" __global__ void clode_features_persistent(const Args a)
 {
     Counters c = {0, 0, 0, 0};
@@ -460,6 +531,8 @@ extern "C" __global__ void clode_features_persistent(const Args a)
     realtype t0 = ZERO, t1 = ZERO;
     Member m;
     Observer o;
+    StepCtl sc;
+    sc.retry = false;
     for (;;) {
         bool want = i < 0 && !exhausted;
         if (want && budget_spent(a, t_start)) {
@@ -507,11 +580,14 @@ extern "C" __global__ void clode_features_persistent(const Args a)
             }
             fresh = rewind = false;
         }
-        bool running = step < a.sp.max_steps && (warm ? m.t < t1 : m.t <= t1);
+        bool running = sc.retry || (step < a.sp.max_steps && (warm ? m.t < t1 : m.t <= t1));
         if (running) {
-            ++step;
-            int flag = step_member(m, a.sp, t1, c);
-            if (warm) {
+            if (!sc.retry)
+                ++step;
+            int flag = step_attempt(m, a.sp, t1, c, sc);
+            if (flag == 1) {
+                // rejected: retried in the next iteration
+            } else if (warm) {
                 o.warmup(m.t, m.x, m.dx, m.aux, a.op);
             } else {
                 hmin_fail |= flag != 0;

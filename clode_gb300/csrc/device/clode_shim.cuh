@@ -94,6 +94,9 @@ __device__ __forceinline__ float minmag(float x, float y) { float ax = fabsf(x),
 __device__ __forceinline__ double minmag(double x, double y) { double ax = fabs(x), ay = fabs(y); return ax < ay ? x : (ay < ax ? y : fmin(x, y)); }
 __device__ __forceinline__ float smoothstep(float e0, float e1, float x) { float t = clamp((x - e0) / (e1 - e0), 0.0f, 1.0f); return t * t * (3.0f - 2.0f * t); }
 __device__ __forceinline__ double smoothstep(double e0, double e1, double x) { double t = clamp((x - e0) / (e1 - e0), 0.0, 1.0); return t * t * (3.0 - 2.0 * t); }
+// OpenCL sincos(x, *cosval) returns the sine and stores the cosine
+__device__ __forceinline__ float sincos(float x, float *c) { float s; sincosf(x, &s, c); return s; }
+__device__ __forceinline__ double sincos(double x, double *c) { double s; ::sincos(x, &s, c); return s; }
 // gamma is what the reference converter emits for Python's math.gamma
 __device__ __forceinline__ float gamma(float x) { return tgammaf(x); }
 __device__ __forceinline__ double gamma(double x) { return tgamma(x); }

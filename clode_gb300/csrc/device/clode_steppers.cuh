@@ -113,6 +113,19 @@ __device__ __forceinline__ int step_member(Member &m, const SolverParams &sp, co
     return 0;
 }
 
+// retry state of a step spread over several calls (adaptive steppers only)
+struct StepCtl {
+    bool retry;
+};
+
+// one attempt of a step; a fixed step never asks for a retry
+__device__ __forceinline__ int step_attempt(Member &m, const SolverParams &sp, const realtype t1, Counters &c,
+                                            StepCtl &s)
+{
+    s.retry = false;
+    return step_member(m, sp, t1, c);
+}
+
 #elif defined(EXPLICIT_BS23) || defined(EXPLICIT_DOPRI5)
 #define CLODE_FIXED_STEP 0
 
@@ -276,6 +289,89 @@ __device__ __forceinline__ int step_member(Member &m, const SolverParams &sp, co
     c.steps++;
     return 0;
 }
+// The same controller as step_member, one attempt per call, so that in the
+// persistent kernels a lane whose attempt is rejected retries in the next
+// iteration of the member loop while the other lanes of its warp go on with
+// their next steps (no warp-wide repeat of the attempt).  Per member the
+// operations and their order are those of step_member.
+struct StepCtl {
+    realtype h;     // step size of the next attempt (before clamping)
+    realtype hmin;  // 16 ulp of t at the start of the step
+    bool retry;     // an attempt of this step was rejected
+    bool first_try;
+};
+
+// returns 0 when the step was accepted, 1 when it was rejected and must be
+// retried (state unchanged), -1 when it failed at hmin (as step_member).
+// Built with CLODE_SPLIT_ATTEMPTS=0 it runs the whole step (step_member) and
+// never asks for a retry; which is faster depends on the model and build.
+__device__ __forceinline__ int step_attempt(Member &m, const SolverParams &sp, const realtype t1, Counters &c,
+                                            StepCtl &s)
+{
+#if !CLODE_SPLIT_ATTEMPTS
+    s.retry = false;
+    return step_member(m, sp, t1, c);
+#endif
+    const realtype safety = RCONST(0.8);
+    const realtype expon = RCONST(1.0) / (CLODE_ERR_ORDER + RCONST(1.0));
+    if (!s.retry) {
+        s.h = m.dt;
+        s.hmin = RCONST(16.0) * fabs(fabs(nextafter(m.t, RCONST(1.1) * t1)) - m.t);
+        s.first_try = true;
+    }
+    const realtype threshold = sp.abstol / sp.reltol;
+    realtype tn = m.t, nerr = ZERO;
+    realtype err[N_VAR], xn[N_VAR], kn[N_VAR];
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j) {
+        xn[j] = m.x[j];
+        kn[j] = m.dx[j];
+    }
+    realtype h = clamp(s.h, s.hmin, sp.dtmax);
+    h = attempt(tn, xn, kn, m.p, h, m.aux, err, m.w);
+    c.rhs += CLODE_RHS_PER_ATTEMPT;
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j)
+        err[j] /= fmax(fmax(fabs(m.x[j]), fabs(xn[j])), threshold);
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j)
+        nerr = fmax(fabs(err[j]), nerr);
+    if (!(nerr > sp.reltol)) {
+        if (s.first_try)
+            h *= fmin(CLODE_MAX_GROW, safety * pow(sp.reltol / nerr, expon));
+        h = fmin(h, t1 - tn);
+        h = clamp(h, s.hmin, sp.dtmax);
+        m.dt = h;
+        m.t = tn;
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            m.x[j] = xn[j];
+            m.dx[j] = kn[j];
+        }
+        c.steps++;
+        s.retry = false;
+        return 0;
+    }
+    c.rejected++;
+    if (h <= s.hmin) {
+        m.dt = s.hmin;
+        c.steps++;
+        s.retry = false;
+        return -1;
+    }
+    if (s.first_try) {
+        s.first_try = false;
+        h *= fmax(CLODE_MAX_SHRINK, safety * pow(sp.reltol / nerr, expon));
+    } else {
+        h *= RCONST(0.5);
+    }
+    s.h = h;
+    s.retry = true;
+    return 1;
+}
+#ifndef CLODE_SPLIT_ATTEMPTS
+#error "CLODE_SPLIT_ATTEMPTS must be defined (0 or 1)"
+#endif
 #else
 #error "no stepper selected: define one of EXPLICIT_EULER, EXPLICIT_HEUN, EXPLICIT_RK4, EXPLICIT_BS23, EXPLICIT_DOPRI5, STOCHASTIC_EULER"
 #endif

@@ -61,6 +61,7 @@ void launch_features(A &a, const clode::NoallocFeaturesLaunch &L, long long n_pt
     a.nPts = (int)n_pts;
     a.i_begin = 0;
     a.i_end = (int)n_pts;
+    a.i_stride = 1;
     a.fused_init = 1;
     a.tspan_pm = (const R *)tspan;
     a.x0 = (const R *)x0;

@@ -197,7 +197,8 @@ struct clode_sim {
     std::string built_key;
     cudaLibrary_t lib = nullptr;
     int lib_device = -1;
-    cudaKernel_t k_transient = nullptr, k_trajectory = nullptr, k_init = nullptr, k_features = nullptr;
+    cudaKernel_t k_transient = nullptr, k_trajectory = nullptr, k_init = nullptr, kp_init = nullptr,
+                 k_features = nullptr;
     cudaKernel_t kp_transient = nullptr, kp_trajectory = nullptr, kp_features = nullptr;
     int last_grid = 0, last_block = 0;
     unsigned int obs_words = 0;
@@ -218,11 +219,13 @@ struct clode_sim {
     bool prec_div = true;
     bool ftz = false;
     bool fast_math = false;
+    bool split_attempts = false;  // persistent kernels: one adaptive attempt per loop iteration
     int maxrregcount = 0;
     double time_budget_ms = 0.0;
-    bool fuse_init = true;
+    bool fuse_init = false;  // separate initialisation launch, as the reference (CLODEfeatures.cpp:180-259)
     bool collect_stats = true;
     long long range_end = -1;  // autotuner trials: run members [0, range_end) only
+    int range_stride = 1;      // ... every range_stride-th of them (persistent kernels)
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -254,6 +257,8 @@ struct clode_sim {
     }
 
     size_t real_size() const { return single ? sizeof(float) : sizeof(double); }
+    bool stepper_adaptive() const { return stepper == "bs23" || stepper == "dopri5"; }
+    bool obs_two_pass() const { return observer == "thresh2" || observer == "nhood2"; }
 
     // --------------------------------------------------------- set-up --
     void set_problem(const clode_problem *p)
@@ -337,7 +342,8 @@ struct clode_sim {
         s.arch = device_arch(device);
         s.defines = {single ? "-DCLODE_SINGLE_PRECISION" : "-DCLODE_DOUBLE_PRECISION", "-D" + kSteppers.at(stepper),
                      "-DN_PAR=" + std::to_string(nPar), "-DN_VAR=" + std::to_string(nVar),
-                     "-DN_AUX=" + std::to_string(nAux), "-DN_WIENER=" + std::to_string(nWiener)};
+                     "-DN_AUX=" + std::to_string(nAux), "-DN_WIENER=" + std::to_string(nWiener),
+                     std::string("-DCLODE_SPLIT_ATTEMPTS=") + (split_attempts ? "1" : "0")};
         if (kind == CLODE_SIM_FEATURES) {
             s.defines.push_back("-D" + kObservers.at(observer));
             s.defines.push_back("-DN_STORE_EVENTS=" + std::to_string(op.max_event_timestamps));
@@ -379,10 +385,12 @@ struct clode_sim {
                        "kernel clode_transient_persistent");
             check_cuda(cudaLibraryGetKernel(&kp_trajectory, lib, "clode_trajectory_persistent"),
                        "kernel clode_trajectory_persistent");
-            k_init = k_features = kp_features = nullptr;
+            k_init = kp_init = k_features = kp_features = nullptr;
             obs_words = 0;
             if (kind == CLODE_SIM_FEATURES) {
                 check_cuda(cudaLibraryGetKernel(&k_init, lib, "clode_init_observer"), "kernel clode_init_observer");
+                check_cuda(cudaLibraryGetKernel(&kp_init, lib, "clode_init_observer_persistent"),
+                           "kernel clode_init_observer_persistent");
                 check_cuda(cudaLibraryGetKernel(&k_features, lib, "clode_features"), "kernel clode_features");
                 check_cuda(cudaLibraryGetKernel(&kp_features, lib, "clode_features_persistent"),
                            "kernel clode_features_persistent");
@@ -551,6 +559,7 @@ struct clode_sim {
         a.nPts = (int)nPts;
         a.i_begin = 0;
         a.i_end = (int)(range_end >= 0 ? std::min(range_end, nPts) : nPts);
+        a.i_stride = range_stride;
         a.t0 = (R)tspan[0];
         a.t1 = (R)tspan[1];
         a.tspan_pm = tspan_per_member ? tspan_dev.as<R>() : nullptr;
@@ -702,7 +711,7 @@ struct clode_sim {
             fail(CLODE_ERR_STATE, "not a feature simulator");
         begin_run();
         resize_features();
-        launch(k_init, nullptr, 0);
+        launch(k_init, kp_init, 0);
         end_run("initializeObserver");
         observer_initialized = true;
         log_msg(CLODE_LOG_DEBUG, "run initializeObserver");
@@ -719,18 +728,23 @@ struct clode_sim {
         resize_features();
         int fused = 0;
         double init_ms = 0.0;
+        unsigned long long init_stats[CLODE_STAT_COUNT] = {0};
         if (!observer_initialized) {
             if (fuse_init) {
                 fused = 1;
             } else {
                 initialize_observer();
                 init_ms = last_ms;
+                memcpy(init_stats, last_stats, sizeof init_stats);
             }
         }
         begin_run();
         launch(k_features, kp_features, fused);
         end_run("features");
+        // time and counters of the whole call, observer initialisation included
         last_ms += init_ms;
+        for (int k = 0; k < CLODE_STAT_COUNT; ++k)
+            last_stats[k] += init_stats[k];
         observer_initialized = true;
         log_msg(CLODE_LOG_DEBUG, "run features");
     }
@@ -795,7 +809,9 @@ struct clode_sim {
         case CLODE_OP_FEATURES:
             if (kind != CLODE_SIM_FEATURES)
                 fail(CLODE_ERR_STATE, "features op on a simulator that is not a feature simulator");
-            launch(k_features, kp_features, obs_init ? 0 : 1);
+            if (!obs_init && !fuse_init)
+                launch(k_init, kp_init, 0);
+            launch(k_features, kp_features, obs_init || !fuse_init ? 0 : 1);
             obs_init = true;
             break;
         case CLODE_OP_TRAJECTORY:
@@ -832,7 +848,8 @@ struct clode_sim {
         if (use_graph) {
             std::ostringstream key;
             key << built_key << "|" << nPts << "|" << tspan[0] << "," << tspan[1] << "|" << tspan_per_member << "|"
-                << schedule << "," << block_size << "," << blocks_per_sm << "," << time_budget_ms << "|" << obs_init
+                << schedule << "," << block_size << "," << blocks_per_sm << "," << time_budget_ms << "," << fuse_init
+                << "|" << obs_init
                 << "|" << collect_stats << "|" << sp.dt << "," << sp.dtmax << "," << sp.abstol << "," << sp.reltol
                 << "," << sp.max_steps << "," << sp.max_store << "," << sp.nout << "|" << op.e_var_ix << ","
                 << op.f_var_ix << "," << op.max_event_count << "," << op.nhood_radius << "," << op.x_up_thresh << ","
@@ -895,72 +912,120 @@ struct clode_sim {
         long long S = std::min(nPts, sample > 0 ? sample : nPts);
         if (S <= 0)
             fail(CLODE_ERR_STATE, "no members to tune on");
+        // a strided sample over the whole ensemble (members 0, k, 2k, ...),
+        // so that it sees every part of a parameter map
+        const int stride = (int)std::max<long long>(1, nPts / S);
         const int cands[][2] = {{0, 128}, {128, 128}, {96, 128}, {80, 128}, {64, 128}, {96, 64}, {80, 64}};
         size_t rs = real_size();
         DevBuf save_dt, save_rng;
-        save_dt.reserve((size_t)S * rs);
-        save_rng.reserve((size_t)S * 2 * sizeof(unsigned long long));
+        save_dt.reserve((size_t)nPts * rs);
+        save_rng.reserve((size_t)nPts * 2 * sizeof(unsigned long long));
         ensure_stream();
         auto snapshot = [&](bool restore) {
             auto cp = [&](void *dst, const void *src, size_t b) {
                 check_cuda(cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, stream), "autotune copy");
             };
-            unsigned long long *r = rng.as<unsigned long long>(), *sr = save_rng.as<unsigned long long>();
             if (!restore) {
-                cp(save_dt.p, dt.p, (size_t)S * rs);
-                cp(sr, r, (size_t)S * 8);
-                cp(sr + S, r + nPts, (size_t)S * 8);
+                cp(save_dt.p, dt.p, (size_t)nPts * rs);
+                cp(save_rng.p, rng.p, (size_t)nPts * 2 * sizeof(unsigned long long));
             } else {
-                cp(dt.p, save_dt.p, (size_t)S * rs);
-                cp(r, sr, (size_t)S * 8);
-                cp(r + nPts, sr + S, (size_t)S * 8);
+                cp(dt.p, save_dt.p, (size_t)nPts * rs);
+                cp(rng.p, save_rng.p, (size_t)nPts * 2 * sizeof(unsigned long long));
             }
         };
         snapshot(false);
+        // one timed run of the sample, then its dt and RNG words restored
+        auto run_trial = [&]() {
+            if (kind == CLODE_SIM_FEATURES) {
+                resize_features();
+                begin_run();
+                if (fuse_init) {
+                    launch(k_features, kp_features, 1);
+                } else {
+                    launch(k_init, kp_init, 0);
+                    launch(k_features, kp_features, 0);
+                }
+            } else if (kind == CLODE_SIM_TRAJECTORY) {
+                resize_trajectory();
+                begin_run();
+                launch(k_trajectory, kp_trajectory, 0);
+            } else {
+                begin_run();
+                launch(k_transient, kp_transient, 0);
+            }
+            end_run("autotune trial");
+            snapshot(true);
+            check_cuda(cudaStreamSynchronize(stream), "autotune restore");
+        };
+        // trials run on the strided sample; the full range is restored on any exit
+        struct SampleRange {
+            clode_sim *sim;
+            SampleRange(clode_sim *s, int stride) : sim(s)
+            {
+                sim->range_end = sim->nPts;
+                sim->range_stride = stride;
+            }
+            ~SampleRange()
+            {
+                sim->range_end = -1;
+                sim->range_stride = 1;
+            }
+        } sample_range(this, stride);
         double best = 1e300;
         int best_regs = maxrregcount, best_block = block_size;
         schedule = 1;
-        range_end = S;
-        try {
-            for (auto &cd : cands) {
-                if (maxrregcount != cd[0]) {
-                    maxrregcount = cd[0];
-                    built = false;
-                }
-                block_size = cd[1];
-                ensure_built();
-                if (kind == CLODE_SIM_FEATURES) {
-                    resize_features();
-                    begin_run();
-                    launch(k_features, kp_features, 1);
-                } else if (kind == CLODE_SIM_TRAJECTORY) {
-                    resize_trajectory();
-                    begin_run();
-                    launch(k_trajectory, kp_trajectory, 0);
-                } else {
-                    begin_run();
-                    launch(k_transient, kp_transient, 0);
-                }
-                end_run("autotune trial");
-                snapshot(true);
-                check_cuda(cudaStreamSynchronize(stream), "autotune restore");
-                log_msg(CLODE_LOG_INFO, "autotune: maxrregcount=%d block=%d: %.3f ms", cd[0], cd[1], last_ms);
-                if (last_ms < best) {
-                    best = last_ms;
-                    best_regs = cd[0];
-                    best_block = cd[1];
-                }
+        for (auto &cd : cands) {
+            if (maxrregcount != cd[0]) {
+                maxrregcount = cd[0];
+                built = false;
             }
-        } catch (...) {
-            range_end = -1;
-            throw;
+            block_size = cd[1];
+            ensure_built();
+            run_trial();
+            log_msg(CLODE_LOG_INFO, "autotune: maxrregcount=%d block=%d: %.3f ms", cd[0], cd[1], last_ms);
+            if (last_ms < best) {
+                best = last_ms;
+                best_regs = cd[0];
+                best_block = cd[1];
+            }
         }
-        range_end = -1;
         if (maxrregcount != best_regs) {
             maxrregcount = best_regs;
             built = false;
         }
         block_size = best_block;
+        // the other stepping variant at the best (register cap, block size)
+        if (stepper_adaptive()) {
+            const bool base_split = split_attempts;
+            split_attempts = !base_split;
+            built = false;
+            ensure_built();
+            run_trial();
+            log_msg(CLODE_LOG_INFO, "autotune: split_attempts=%d: %.3f ms", (int)split_attempts, last_ms);
+            if (last_ms < best) {
+                best = last_ms;
+            } else {
+                split_attempts = base_split;
+                built = false;
+            }
+        }
+        // fused or separate observer initialisation (two-pass observers)
+        if (kind == CLODE_SIM_FEATURES && obs_two_pass()) {
+            ensure_built();
+            const bool base_fuse = fuse_init;
+            fuse_init = !base_fuse;
+            try {
+                run_trial();
+            } catch (...) {
+                fuse_init = base_fuse;
+                throw;
+            }
+            log_msg(CLODE_LOG_INFO, "autotune: fuse_init=%d: %.3f ms", (int)fuse_init, last_ms);
+            if (last_ms < best)
+                best = last_ms;
+            else
+                fuse_init = base_fuse;
+        }
         observer_initialized = false;
         ensure_built();
         if (best_ms_out)
@@ -1492,9 +1557,12 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 sim->fmad = v;
                 sim->built = false;
             }
-        } else if (k == "prec_div" || k == "ftz" || k == "fast_math") {
+        } else if (k == "prec_div" || k == "ftz" || k == "fast_math" || k == "split_attempts") {
             bool v = value != 0.0;
-            bool &field = k == "prec_div" ? sim->prec_div : (k == "ftz" ? sim->ftz : sim->fast_math);
+            bool &field = k == "prec_div" ? sim->prec_div
+                          : k == "ftz"    ? sim->ftz
+                          : k == "fast_math" ? sim->fast_math
+                                             : sim->split_attempts;
             if (v != field) {
                 field = v;
                 sim->built = false;
@@ -1532,6 +1600,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "prec_div") *value = sim->prec_div;
         else if (k == "ftz") *value = sim->ftz;
         else if (k == "fast_math") *value = sim->fast_math;
+        else if (k == "split_attempts") *value = sim->split_attempts;
         else if (k == "maxrregcount") *value = sim->maxrregcount;
         else if (k == "time_budget_ms") *value = sim->time_budget_ms;
         else if (k == "fuse_init") *value = sim->fuse_init;

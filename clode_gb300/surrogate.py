@@ -207,10 +207,29 @@ class FeatureMapScreen:
                 best = (float(r_s[j]), float(tv), frac)
         return best
 
+    @staticmethod
+    def _cell_stats(E, P, scale):
+        """Per cell of a lattice of exact values E and predictions P (both
+        [rows, cols, K], NaN where unknown): the network's worst miss on the
+        four corners and the corners' spread, in units of the feature range.
+        Cells with an unknown corner get NaN (never accepted)."""
+        R = (np.abs(P - E) / scale).max(axis=2)
+        c = lambda A: (A[:-1, :-1], A[:-1, 1:], A[1:, :-1], A[1:, 1:])
+        r_cell = np.maximum.reduce(c(R))
+        v_cell = ((np.maximum.reduce(c(E)) - np.minimum.reduce(c(E))) / scale).max(axis=2)
+        return r_cell, v_cell
+
     def run(self, nx: int, ny: int, train_stride: int = 8, steps: int = 3000, batch: int = 4096,
-            lr: float = 2e-3, tol: float = 0.01, keep: float = 0.99, n_calibration: int = 65536) -> ScreenResult:
+            lr: float = 2e-3, tol: float = 0.01, keep: float = 0.99, n_calibration: int = 65536,
+            refine: bool = False) -> ScreenResult:
         """Screened map of the nx x ny grid (point m = iy * nx + ix); features
-        are float32 (the FP32 engine's values are exact in float32)."""
+        are float32 (the FP32 engine's values are exact in float32).
+
+        With `refine`, a rejected cell is not integrated whole: its midpoint
+        lattice is integrated, the cell splits into four sub-cells, and those
+        are screened again with thresholds calibrated on a second sample drawn
+        from the rejected cells; only the points of rejected sub-cells fall
+        back to the engine."""
         t_all = time.perf_counter()
         K = self.K
         g0 = np.linspace(self.lo[0], self.hi[0], nx)
@@ -238,6 +257,11 @@ class FeatureMapScreen:
         t0 = time.perf_counter()
         F = self.net.predict_grid(nx, ny, sd, mu)
         t_predict = time.perf_counter() - t0
+        # the lattice of the sub-grid lines and their midlines, for the refinement
+        sx2 = np.unique(np.r_[sx, (sx[:-1] + sx[1:]) // 2])
+        sy2 = np.unique(np.r_[sy, (sy[:-1] + sy[1:]) // 2])
+        refine = refine and sx.size > 1 and sy.size > 1
+        P2 = F.reshape(ny, nx, K)[np.ix_(sy2, sx2)].astype(np.float64) if refine else None
         # 4. cell statistics from the integrated corners
         t0 = time.perf_counter()
         Fs = Fsub.reshape(sy.size, sx.size, K)
@@ -277,15 +301,54 @@ class FeatureMapScreen:
             F[cal] = Fcal
             flags[cal] = ScreenResult.SAMPLED
         t_cal = time.perf_counter() - t0
-        # 6. fallback: the plain engine on every point of a rejected cell
+        # 6. cells that fail the screen
         t0 = time.perf_counter()
-        reject_cell = (r_cell > tr) | (v_cell > tv)
+        reject_cell = ~((r_cell <= tr) & (v_cell <= tv))
         reject = reject_cell[cy[:, None], cx[None, :]].ravel() & (flags == ScreenResult.SURROGATE)
         redo = np.nonzero(reject)[0]
+        t_refine, tr2, tv2, acc2, n_lattice, n_cal2 = 0.0, -1.0, -1.0, 0.0, 0, 0
+        if refine and redo.size:
+            # 6a. the midpoint lattice of every rejected cell
+            t1 = time.perf_counter()
+            ry, rx = np.nonzero(reject_cell)
+            xs3 = np.stack([sx[rx], (sx[rx] + sx[rx + 1]) // 2, sx[rx + 1]], axis=1)
+            ys3 = np.stack([sy[ry], (sy[ry] + sy[ry + 1]) // 2, sy[ry + 1]], axis=1)
+            lat = np.unique((ys3[:, :, None] * nx + xs3[:, None, :]).ravel())
+            new_pts = lat[flags[lat] == ScreenResult.SURROGATE]
+            if new_pts.size:
+                F[new_pts] = np.asarray(self.integrate(g0[new_pts % nx], g1[new_pts // nx]), dtype=np.float64)
+                flags[new_pts] = ScreenResult.SAMPLED
+            n_lattice = int(new_pts.size)
+            E2 = np.full((sy2.size, sx2.size, K), np.nan)
+            li, lj = np.searchsorted(sx2, lat % nx), np.searchsorted(sy2, lat // nx)
+            E2[lj, li] = F[lat]
+            r2_cell, v2_cell = self._cell_stats(E2, P2, scale)
+            cx2 = np.clip(np.searchsorted(sx2, np.arange(nx), side="right") - 1, 0, sx2.size - 2)
+            cy2 = np.clip(np.searchsorted(sy2, np.arange(ny), side="right") - 1, 0, sy2.size - 2)
+            # 6b. second calibration sample, from the rejected cells' remaining points
+            cand = np.nonzero(reject & (flags == ScreenResult.SURROGATE))[0]
+            cal2 = rng.choice(cand, size=min(max(n_calibration // 2, 1), cand.size), replace=False) \
+                if cand.size else np.zeros(0, dtype=np.int64)
+            if cal2.size:
+                ix2, iy2 = cal2 % nx, cal2 // nx
+                Fc2 = np.asarray(self.integrate(g0[ix2], g1[iy2]), dtype=np.float64)
+                err2 = self.map_error(F[cal2], Fc2, scale)
+                r2s, v2s = r2_cell[cy2[iy2], cx2[ix2]], v2_cell[cy2[iy2], cx2[ix2]]
+                known = np.isfinite(r2s) & np.isfinite(v2s)
+                tr2, tv2, acc2 = self._calibrate(r2s[known], v2s[known], err2[known], tol, keep)
+                F[cal2] = Fc2
+                flags[cal2] = ScreenResult.SAMPLED
+            n_cal2 = int(cal2.size)
+            # 6c. keep the sub-cells that pass
+            sub_ok = (r2_cell <= tr2) & (v2_cell <= tv2)
+            keep_pt = sub_ok[cy2[:, None], cx2[None, :]].ravel()
+            redo = np.nonzero(reject & (flags == ScreenResult.SURROGATE) & ~keep_pt)[0]
+            t_refine = time.perf_counter() - t1
+        # 7. fallback: the plain engine on every point that is still rejected
         if redo.size:
             F[redo] = np.asarray(self.integrate(g0[redo % nx], g1[redo // nx]), dtype=np.float64)
             flags[redo] = ScreenResult.FALLBACK
-        t_fallback = time.perf_counter() - t0
+        t_fallback = time.perf_counter() - t0 - t_refine
         total = time.perf_counter() - t_all
         return ScreenResult(F, flags, loss=loss, timings={
             "train_data_s": t_train_data, "train_s": t_train, "predict_s": t_predict, "cells_s": t_cells,
@@ -293,4 +356,6 @@ class FeatureMapScreen:
             "points_per_s": nx * ny / total, "training_points": int(sub.size), "calibration_points": int(cal.size),
             "fallback_points": int(redo.size), "integrated_points": int(np.count_nonzero(flags)),
             "r_max": tr, "v_max": tv, "calibrated_accept_fraction": acc, "rejected_cells": int(reject_cell.sum()),
-            "cells": int(reject_cell.size), "feature_scale": scale.tolist()})
+            "cells": int(reject_cell.size), "refine_s": t_refine, "lattice_points": n_lattice,
+            "calibration2_points": n_cal2, "r2_max": tr2, "v2_max": tv2, "calibrated_accept_fraction2": acc2,
+            "feature_scale": scale.tolist()})

@@ -233,9 +233,17 @@ int clode_sim_get_stats(clode_sim *sim, unsigned long long *out);
 int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
 /* Engine options: "schedule" (0 grid, 1 persistent), "block_size", "blocks_per_sm",
  * "fmad" (0/1: allow contraction of a*b+c; 0 reproduces the reference bit for bit),
+ * "prec_div" (1: IEEE division, 0: approximate), "ftz" (1: flush FP32 denormals),
+ * "fast_math" (1: approximate exp/log/pow/sin/cos/sqrt, implies prec_div 0 and ftz 1),
+ * "maxrregcount" (0: no cap, else 32..255 registers per thread),
+ * "split_attempts" (adaptive steppers, persistent kernels: 1 = one step attempt per
+ * loop iteration, a rejected attempt retried in the next; results are identical),
  * "time_budget_ms" (persistent launches stop taking new members after it),
- * "fuse_init" (0/1: run the observer initialisation inside the features launch),
- * "collect_stats" (0/1). */
+ * "fuse_init" (0/1, default 0: run the observer initialisation inside the features
+ * launch instead of a launch of its own before it; results are identical),
+ * "collect_stats" (0/1).  Read-only for get_option: "last_grid", "last_block".
+ * Changing a build option (fmad, prec_div, ftz, fast_math, maxrregcount,
+ * split_attempts) recompiles the program at the next run. */
 int clode_sim_set_option(clode_sim *sim, const char *key, double value);
 int clode_sim_get_option(clode_sim *sim, const char *key, double *value);
 /* Chains: ops run back to back on the simulator's stream, one synchronisation
@@ -248,8 +256,12 @@ int clode_sim_chain(clode_sim *sim, const int *ops, int n_ops, int use_graph);
 /* Autotuner: times the persistent kernel of this simulator's kind on members
  * [0, sample) (sample <= 0: all) for register caps {none, 128, 96, 80, 64} and
  * block sizes {64, 128}, keeps the fastest ("maxrregcount", "block_size",
- * schedule 1) and returns its time.  The sampled members' dt and RNG state are
- * restored; the observer is re-initialised at the next features run. */
+ * schedule 1), then for adaptive steppers also times the other value of the
+ * "split_attempts" option at that pair and keeps the faster, for two-pass
+ * observers (nhood2, thresh2) also the other value of "fuse_init", and
+ * returns the best time.  Numerics options are not changed.  The sampled members' dt and
+ * RNG state are restored; the observer is re-initialised at the next
+ * features run. */
 int clode_sim_autotune(clode_sim *sim, long long sample, double *best_ms);
 /* Number of kernel launches this library has issued since it was loaded
  * (ensemble kernels and the conversion/seeding kernels alike). */

@@ -183,7 +183,8 @@ PERSISTENT = {"schedule": 1}
 
 @pytest.mark.parametrize("observer", ["localmax", "nhood2", "thresh2"])
 @pytest.mark.parametrize("single", [False, True])
-def test_persistent_schedule_bitwise(observer, single):
+@pytest.mark.parametrize("fuse", [1, 0])
+def test_persistent_schedule_bitwise(observer, single, fuse):
     # uneven members: per-member time spans over a factor of 20
     x0, p = lorenz_inputs(2000)
     rng = np.random.default_rng(3)
@@ -192,8 +193,8 @@ def test_persistent_schedule_bitwise(observer, single):
                   sp=dict(dt=0.005, max_steps=100000),
                   op=dict(e_var_ix=2, f_var_ix=2, max_event_count=10000, x_up_threshold=0.3, x_down_threshold=0.2,
                           nhood_radius=0.1),
-                  tspan_pm=tspan, steps=[("features",), ("shift_x0",), ("features",)])
-    eng, ora = run_engine(sc, options=PERSISTENT), run_oracle(sc)
+                  tspan_pm=tspan, steps=[("features",), ("shift_x0",), ("features",), ("features", None, True)])
+    eng, ora = run_engine(sc, options=dict(PERSISTENT, fuse_init=fuse)), run_oracle(sc)
     assert_bitwise(eng, ora)
 
 
@@ -208,6 +209,35 @@ def test_persistent_transient_trajectory_bitwise(kind):
     eng, ora = run_engine(sc, options=PERSISTENT), run_oracle(sc)
     keys = ("xf", "tf", "dt") + (("t", "x", "dx", "n_stored") if kind == "trajectory" else ())
     assert_bitwise(eng, ora, keys=keys)
+
+
+@pytest.mark.parametrize("stepper", ["bs23", "dopri5"])
+@pytest.mark.parametrize("kind", ["features", "transient", "trajectory"])
+def test_split_attempts_bitwise(stepper, kind):
+    # adaptive steps with rejections: one attempt per loop iteration
+    # (split_attempts 1) gives the same results as whole steps, on both
+    # schedules, since each member's operations are unchanged (fmad off: with
+    # contraction allowed the compiler may fuse differently in each kernel)
+    x0, p = lorenz_inputs(1500)
+    rng = np.random.default_rng(6)
+    tspan = np.stack([np.zeros(1500), rng.uniform(2.0, 12.0, 1500)], axis=1)
+    steps = {"features": [("features",), ("shift_x0",), ("features",)],
+             "transient": [("transient",), ("shift_x0",), ("transient",)],
+             "trajectory": [("trajectory",)]}[kind]
+    sc = Scenario("lorenz.cl", 3, 3, x0, p, n_aux=1, stepper=stepper, observer="thresh2" if kind == "features" else None,
+                  single=True, sp=dict(dt=0.05, dtmax=0.5, abstol=1e-7, reltol=1e-5, max_steps=200000,
+                                      max_store=2000, nout=3),
+                  op=dict(e_var_ix=2, f_var_ix=2, max_event_count=10000, x_up_threshold=0.3, x_down_threshold=0.2),
+                  tspan_pm=tspan, steps=steps)
+    assert sc.kind == kind
+    ref = run_engine(sc, options={"schedule": 0, "fmad": 0})
+    assert ref["stats"][0]["rejected"] > 0
+    for opts in ({"schedule": 1, "fmad": 0, "split_attempts": 0}, {"schedule": 1, "fmad": 0, "split_attempts": 1},
+                 {"schedule": 1, "fmad": 0, "split_attempts": 1, "fuse_init": 0}):
+        eng = run_engine(sc, options=opts)
+        keys = ("xf", "tf", "dt") + (("t", "x", "dx", "n_stored") if kind == "trajectory" else ())
+        assert_bitwise(eng, ref, keys=keys)  # and every features run
+        assert eng["stats"][0]["rejected"] == ref["stats"][0]["rejected"]
 
 
 def test_persistent_stochastic_bitwise_rng_state():

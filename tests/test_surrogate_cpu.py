@@ -3,6 +3,7 @@ sub-grid / calibration / fallback bookkeeping and the calibrated cell screen,
 with an analytic map standing in for the engine and a stand-in network whose
 error is known (no GPU involved)."""
 import numpy as np
+import pytest
 
 from clode_gb300.surrogate import FeatureMapScreen, ScreenResult
 
@@ -52,11 +53,13 @@ def _screen(calls):
     return scr
 
 
-def test_screened_map_bookkeeping_and_error():
+@pytest.mark.parametrize("refine", [False, True])
+def test_screened_map_bookkeeping_and_error(refine):
     calls = []
     scr = _screen(calls)
     nx, ny = 200, 150
-    res = scr.run(nx, ny, train_stride=8, steps=40, batch=64, tol=0.01, keep=0.99, n_calibration=3000)
+    res = scr.run(nx, ny, train_stride=8, steps=40, batch=64, tol=0.01, keep=0.99, n_calibration=3000,
+                  refine=refine)
     g0, g1 = np.linspace(0, 1, nx), np.linspace(0, 1, ny)
     P0, P1 = np.meshgrid(g0, g1, indexing="xy")
     exact = _map(P0.ravel(), P1.ravel())
@@ -65,8 +68,12 @@ def test_screened_map_bookkeeping_and_error():
     assert t["training_points"] == len(np.unique(np.r_[0:nx:8, nx - 1])) * len(np.unique(np.r_[0:ny:8, ny - 1]))
     assert t["calibration_points"] == 3000
     assert calls[0] == t["training_points"] and calls[1] == 3000
-    assert t["integrated_points"] == t["training_points"] + 3000 + t["fallback_points"]
-    assert np.count_nonzero(res.flags == ScreenResult.SAMPLED) == t["training_points"] + 3000
+    sampled = t["training_points"] + 3000 + t["lattice_points"] + t["calibration2_points"]
+    assert t["integrated_points"] == sampled + t["fallback_points"]
+    assert np.count_nonzero(res.flags == ScreenResult.SAMPLED) == sampled
+    assert np.count_nonzero(res.flags == ScreenResult.FALLBACK) == t["fallback_points"]
+    if not refine:
+        assert t["lattice_points"] == 0 and t["calibration2_points"] == 0
     # every integrated point carries the engine's value
     integ = res.flags != ScreenResult.SURROGATE
     np.testing.assert_array_equal(res.features[integ], exact[integ].astype(np.float32))
