@@ -44,6 +44,11 @@ N_VAR, N_PAR, N_AUX = 4, 3, 1
 FLOPS_PER_RHS = 43              # + - * / in the lactotroph RHS (3 exp counted apart)
 FLOPS_PER_ATTEMPT = 62 * N_VAR + 10   # DP45 stage combinations and error norm
 FLOPS_PER_STEP_OBS = 5 * N_VAR + 3 * N_AUX + 6  # nhood2 per-step extrema and means
+# DRAM bytes (read + write) per member of one map (warm-up launch + feature
+# launch): ncu dram__bytes_{read,write}.sum of both launches on the 512 x 512
+# case (262,144 members: 100.3 MB + 360.8 MB), scaled by members; the traffic
+# is per-member state, so it grows in proportion
+DRAM_BYTES_PER_MEMBER = (52592384 + 47750912 + 129954560 + 230851840) / 262144
 
 
 def make_workload(grid: int, seed: int, tmin: float, tmax: float, rank: int = 0):
@@ -315,6 +320,7 @@ def main():
     ap.add_argument("--prec-div", type=int, default=0)
     ap.add_argument("--ftz", type=int, default=1)
     ap.add_argument("--fast-math", type=int, default=0, help="approximate exp/pow/sqrt (NVRTC --use_fast_math)")
+    ap.add_argument("--fast-exp", type=int, default=0, help="the model's FP32 exp within 2.5 ulp (own Cody-Waite exp)")
     ap.add_argument("--maxrreg", type=int, default=None)
     ap.add_argument("--blocks-per-sm", type=int, default=None)
     ap.add_argument("--autotune", type=int, default=262144, help="autotune on this many members first (0: off)")
@@ -353,6 +359,7 @@ def main():
     sim.set_option("schedule", args.schedule)
     sim.set_option("block_size", args.block_size)
     for key, val in (("prec_div", args.prec_div), ("ftz", args.ftz), ("fast_math", args.fast_math),
+                     ("fast_exp", args.fast_exp),
                      ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm)):
         if val is not None:
             sim.set_option(key, val)
@@ -450,7 +457,7 @@ def main():
                    "schedule": "persistent" if sim.get_option("schedule") else "grid",
                    "block_size": args.block_size, "fmad": bool(args.fmad),
                    "variant": {k: v for k, v in (("prec_div", args.prec_div), ("ftz", args.ftz),
-                                                 ("fast_math", args.fast_math),
+                                                 ("fast_math", args.fast_math), ("fast_exp", args.fast_exp),
                                                  ("maxrregcount", args.maxrreg),
                                                  ("blocks_per_sm", args.blocks_per_sm)) if v is not None},
                    "registers": sim.kernel_registers("features_persistent" if sim.get_option("schedule") else "features"),
@@ -462,7 +469,8 @@ def main():
         "stats_per_step": st,
         "wall_ms_per_step_device_loop": 1e3 * wall_dev / args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
-                     "frac": achieved_tflops / peak_tflops, "traffic": None,
+                     "frac": achieved_tflops / peak_tflops, "traffic": DRAM_BYTES_PER_MEMBER * n,
+                     "traffic_source": "ncu DRAM bytes of the 512 x 512 map (both launches), scaled by members",
                      "peak_source": f"nominal FP32 FMA rate {info.compute_units} SMs x 128 lanes x 2 at the "
                                     f"median sampled SM clock {sm_mhz:.0f} MHz",
                      "flops_per_launch": flops},
@@ -490,7 +498,7 @@ def main():
                                 "mean_period_rel_err_median": float(np.median(rel)),
                                 "mean_period_rel_err_p99": float(np.quantile(rel, 0.99))}
     opts = {k: sim.get_option(k) for k in ("schedule", "block_size", "maxrregcount", "fmad", "prec_div", "ftz",
-                                           "fast_math")}
+                                           "fast_math", "fast_exp", "split_attempts", "fuse_init")}
     if rank == 0 and not args.no_surrogate:
         try:
             line["surrogate"] = bench_surrogate(args, opts)

@@ -101,6 +101,31 @@ __device__ __forceinline__ double sincos(double x, double *c) { double s; ::sinc
 __device__ __forceinline__ float gamma(float x) { return tgammaf(x); }
 __device__ __forceinline__ double gamma(double x) { return tgamma(x); }
 
+// Optional faster FP32 exp (build define CLODE_FAST_EXP=1, simulator option
+// "fast_exp"): Cody-Waite splitting of x * log2(e) into the rounded product
+// y and its exact remainder r (two fma), 2^y from the hardware base-2
+// exponential, times (1 + r ln 2).  Within a few ulp of the correctly rounded
+// result over the normal range (tested against CUDA's expf); where 2^y
+// overflows or underflows the hardware result (inf, 0) is returned as is.
+// FP64 keeps exp().
+#if defined(CLODE_FAST_EXP) && CLODE_FAST_EXP
+__device__ __forceinline__ float clode_exp_f32(float x)
+{
+    const float l2e_hi = 1.44269502162933349609375f;  // log2(e) rounded to FP32
+    const float l2e_lo = 1.925963033500011e-08f;       // log2(e) - l2e_hi
+    const float y = x * l2e_hi;
+    float r = fmaf(x, l2e_hi, -y);
+    r = fmaf(x, l2e_lo, r);
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(y));
+    const float corr = fmaf(e, r * 0.693147182464599609375f, e);
+    return fabsf(y) < 128.0f ? corr : e;  // beyond: inf or 0, where the correction would give NaN
+}
+__device__ __forceinline__ float clode_exp(float x) { return clode_exp_f32(x); }
+__device__ __forceinline__ double clode_exp(double x) { return ::exp(x); }
+#define exp(x) clode_exp(x)
+#endif
+
 // native_* and half_* variants map to the accurate functions
 #define native_exp exp
 #define native_exp2 exp2

@@ -162,15 +162,19 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
 //   EPI_MUL_BF16:   Y = . * mask[m, n]          -> BF16 core-matrix order (no bias)
 enum { EPI_RELU_BF16 = 0, EPI_BIAS_F32 = 1, EPI_MASK_BF16 = 2, EPI_MUL_BF16 = 3 };
 
-template <int K, int N, int EPI>
+// The N output columns are split in N / NS slices of NS columns; CTA c owns
+// slice c % (N / NS) (its NS x K weight rows stay in shared memory) and
+// walks the row tiles c / (N / NS), + gridDim.x / (N / NS), ...
+template <int K, int N, int EPI, int NS>
 __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X, int M, const bf16 *__restrict__ B,
                                                        const float *__restrict__ bias,
                                                        const bf16 *__restrict__ mask, void *__restrict__ Y,
                                                        int *__restrict__ err)
 {
-    static_assert(K % 16 == 0 && N % 16 == 0 && N >= 16 && N <= 256, "tile shape");
-    constexpr uint32_t kCols = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
-    constexpr uint32_t kABytes = kTileM * K * 2, kBBytes = N * K * 2;
+    static_assert(K % 16 == 0 && N % NS == 0 && NS % 16 == 0 && NS >= 16 && NS <= 256, "tile shape");
+    constexpr int kSlices = N / NS;
+    constexpr uint32_t kCols = NS <= 32 ? 32 : (NS <= 64 ? 64 : (NS <= 128 ? 128 : 256));
+    constexpr uint32_t kABytes = kTileM * K * 2, kBBytes = NS * K * 2;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *sA = smem;             // kTileM x K bf16, core-matrix order
     unsigned char *sB = smem + kABytes;   // N x K bf16, core-matrix order
@@ -181,7 +185,9 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles = (M + kTileM - 1) / kTileM;
-    int tile = blockIdx.x;
+    const int slice = blockIdx.x % kSlices, col0 = slice * NS;
+    const int tile_step = gridDim.x / kSlices;
+    int tile = blockIdx.x / kSlices;
     if (warp == 0)
         tmem_alloc(tslot, kCols);
     if (tid == 0) {
@@ -189,9 +195,9 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
         mbar_init(bar_mma, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *sflag = 0;
-        if (tile < tiles) {  // the weights and the first tile arrive on the first phase
+        if (tile < tiles) {  // the weight slice and the first tile arrive on the first phase
             mbar_expect_tx(bar_ld, kBBytes + kABytes);
-            bulk_g2s(sB, B, kBBytes, bar_ld);
+            bulk_g2s(sB, B + (size_t)col0 * K, kBBytes, bar_ld);
             bulk_g2s(sA, X + (size_t)tile * kTileM * K, kABytes, bar_ld);
         }
     }
@@ -199,12 +205,12 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    const uint32_t idesc = idesc_bf16(kTileM, N);
+    const uint32_t idesc = idesc_bf16(kTileM, NS);
     uint32_t ph_ld = 0, ph_mma = 0;
     int pending = 0;  // thread 0: 1 = a copy may be in flight, 2 = an MMA group may be in flight
     bool failed = false;
 
-    for (; tile < tiles; tile += gridDim.x) {
+    for (; tile < tiles; tile += tile_step) {
         const int row0 = tile * kTileM;
         if (tid == 0) {
             int st = 0;
@@ -224,7 +230,7 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
                     pending = 2;
                 } else {
                     // the MMA group has consumed sA: fetch the next tile behind the epilogue
-                    const int next = tile + gridDim.x;
+                    const int next = tile + tile_step;
                     if (next < tiles) {
                         mbar_expect_tx(bar_ld, kABytes);
                         bulk_g2s(sA, X + (size_t)next * kTileM * K, kABytes, bar_ld);
@@ -246,9 +252,10 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
         const int m = row0 + warp * 32 + lane;
         const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
-        for (int c0 = 0; c0 < N; c0 += 16) {
+        for (int c = 0; c < NS; c += 16) {
+            const int c0 = col0 + c;  // column in the full output
             float v[16];
-            tmem_ld16(trow + (uint32_t)c0, v);
+            tmem_ld16(trow + (uint32_t)c, v);
             if (m >= M && EPI != EPI_BIAS_F32) {
                 // rows past M in the last tile are zero, so that batch
                 // reductions over whole tiles see nothing there
@@ -305,26 +312,43 @@ __global__ void __launch_bounds__(128, 1) k_linear_tc(const bf16 *__restrict__ X
         tmem_dealloc(tmem, kCols);
 }
 
-template <int K, int N, int EPI>
-size_t linear_smem_bytes()
+// NS: output columns per CTA
+template <int K, int N, int EPI, int NS>
+void launch_linear_ns(const bf16 *X, int M, const bf16 *B, const float *bias, const bf16 *mask, void *Y, int *err,
+                      int sms, cudaStream_t s)
 {
-    return (size_t)kTileM * K * 2 + (size_t)N * K * 2 + 64;
+    constexpr int kSlices = N / NS;
+    const size_t smem = (size_t)kTileM * K * 2 + (size_t)NS * K * 2 + 64;
+    check_cuda(cudaFuncSetAttribute(k_linear_tc<K, N, EPI, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem),
+               "tensor-core layer shared memory");
+    const int tiles = (M + kTileM - 1) / kTileM;
+    int per_slice = sms / kSlices;  // CTAs per column slice
+    if (per_slice < 1)
+        per_slice = 1;
+    if (per_slice > tiles)
+        per_slice = tiles;
+    k_linear_tc<K, N, EPI, NS><<<per_slice * kSlices, 128, smem, s>>>(X, M, B, bias, mask, Y, err);
+    count_launch();
+    check_cuda(cudaGetLastError(), "tensor-core layer launch");
 }
 
+// Few row tiles (a training batch): the 256 output columns split over 4 CTAs
+// per tile, so that the layer occupies 4x as many SMs.  Many row tiles (a
+// grid prediction): one CTA per tile and all columns, so each activation tile
+// is read once.
 template <int K, int N, int EPI>
 void launch_linear(const bf16 *X, int M, const bf16 *B, const float *bias, const bf16 *mask, void *Y, int *err,
                    int sms, cudaStream_t s)
 {
     if (M <= 0)
         return;
-    size_t smem = linear_smem_bytes<K, N, EPI>();
-    check_cuda(cudaFuncSetAttribute(k_linear_tc<K, N, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-               "tensor-core layer shared memory");
-    int tiles = (M + kTileM - 1) / kTileM;
-    int grid = tiles < sms ? tiles : sms;
-    k_linear_tc<K, N, EPI><<<grid, 128, smem, s>>>(X, M, B, bias, mask, Y, err);
-    count_launch();
-    check_cuda(cudaGetLastError(), "tensor-core layer launch");
+    constexpr int kNarrow = N > 64 ? 64 : N;
+    const int tiles = (M + kTileM - 1) / kTileM;
+    if (kNarrow < N && tiles < sms)
+        launch_linear_ns<K, N, EPI, kNarrow>(X, M, B, bias, mask, Y, err, sms, s);
+    else
+        launch_linear_ns<K, N, EPI, N>(X, M, B, bias, mask, Y, err, sms, s);
 }
 
 // ---------------------------------------------------------- CUDA-core parts --
@@ -814,11 +838,11 @@ void mse(const float *out, const float *y, int M, int H, int K, bf16 *dz, float 
 }
 
 namespace {
-int rows_per_block_for(int M, int max_blocks_z)
+int rows_per_block_for(int M, int max_blocks)
 {
-    int r = (M + max_blocks_z - 1) / max_blocks_z;
-    r = (r + 31) / 32 * 32;
-    return r < 64 ? 64 : r;
+    int r = (M + max_blocks - 1) / max_blocks;
+    r = (r + 15) / 16 * 16;
+    return r < 16 ? 16 : r;
 }
 }  // namespace
 
@@ -840,7 +864,7 @@ void weight_grad_input(const float *x, const bf16 *D, int M, float *G, float *g,
 {
     if (M <= 0)
         return;
-    const int rpb = rows_per_block_for(M, 64);
+    const int rpb = rows_per_block_for(M, 256);
     k_weight_grad_input<<<(unsigned int)((M + rpb - 1) / rpb), kWidth, 0, s>>>(x, D, M, rpb, G, g);
     after_launch("input-layer gradient launch");
 }

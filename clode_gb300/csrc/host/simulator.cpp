@@ -219,6 +219,7 @@ struct clode_sim {
     bool prec_div = true;
     bool ftz = false;
     bool fast_math = false;
+    bool fast_exp = false;        // FP32 exp and controller pow of a few ulp (CLODE_FAST_EXP)
     bool split_attempts = false;  // persistent kernels: one adaptive attempt per loop iteration
     int maxrregcount = 0;
     double time_budget_ms = 0.0;
@@ -343,7 +344,8 @@ struct clode_sim {
         s.defines = {single ? "-DCLODE_SINGLE_PRECISION" : "-DCLODE_DOUBLE_PRECISION", "-D" + kSteppers.at(stepper),
                      "-DN_PAR=" + std::to_string(nPar), "-DN_VAR=" + std::to_string(nVar),
                      "-DN_AUX=" + std::to_string(nAux), "-DN_WIENER=" + std::to_string(nWiener),
-                     std::string("-DCLODE_SPLIT_ATTEMPTS=") + (split_attempts ? "1" : "0")};
+                     std::string("-DCLODE_SPLIT_ATTEMPTS=") + (split_attempts ? "1" : "0"),
+                     std::string("-DCLODE_FAST_EXP=") + (fast_exp ? "1" : "0")};
         if (kind == CLODE_SIM_FEATURES) {
             s.defines.push_back("-D" + kObservers.at(observer));
             s.defines.push_back("-DN_STORE_EVENTS=" + std::to_string(op.max_event_timestamps));
@@ -1557,11 +1559,12 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 sim->fmad = v;
                 sim->built = false;
             }
-        } else if (k == "prec_div" || k == "ftz" || k == "fast_math" || k == "split_attempts") {
+        } else if (k == "prec_div" || k == "ftz" || k == "fast_math" || k == "fast_exp" || k == "split_attempts") {
             bool v = value != 0.0;
-            bool &field = k == "prec_div" ? sim->prec_div
-                          : k == "ftz"    ? sim->ftz
+            bool &field = k == "prec_div"    ? sim->prec_div
+                          : k == "ftz"       ? sim->ftz
                           : k == "fast_math" ? sim->fast_math
+                          : k == "fast_exp"  ? sim->fast_exp
                                              : sim->split_attempts;
             if (v != field) {
                 field = v;
@@ -1600,6 +1603,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "prec_div") *value = sim->prec_div;
         else if (k == "ftz") *value = sim->ftz;
         else if (k == "fast_math") *value = sim->fast_math;
+        else if (k == "fast_exp") *value = sim->fast_exp;
         else if (k == "split_attempts") *value = sim->split_attempts;
         else if (k == "maxrregcount") *value = sim->maxrregcount;
         else if (k == "time_budget_ms") *value = sim->time_budget_ms;

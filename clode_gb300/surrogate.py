@@ -359,3 +359,38 @@ class FeatureMapScreen:
             "cells": int(reject_cell.size), "refine_s": t_refine, "lattice_points": n_lattice,
             "calibration2_points": n_cal2, "r2_max": tr2, "v2_max": tv2, "calibrated_accept_fraction2": acc2,
             "feature_scale": scale.tolist()})
+
+
+def _speed(steps: int, batch: int, grid: int, seed: int) -> dict:
+    """Training-step and grid-prediction timings of the network on synthetic
+    smooth targets (262,144 training rows)."""
+    net = MLP(4, 4, 0, seed)
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, (262144, 2)).astype(np.float32)
+    y = np.stack([np.sin(3 * x[:, 0]) * np.cos(2 * x[:, 1]), x[:, 0] * x[:, 1], np.exp(-x[:, 0] ** 2),
+                  x[:, 1] ** 3], axis=1).astype(np.float32)
+    net.train(x, y, steps=5, batch=batch)  # kernel attributes, graph capture
+    hist = net.train(x, y, steps=steps, batch=batch)
+    train_ms, _ = net.timings()
+    net.predict_grid(64, 64)
+    t0 = time.perf_counter()
+    net.predict_grid(grid, grid)
+    wall = time.perf_counter() - t0
+    _, pred_ms = net.timings()
+    return {"steps": steps, "batch": batch, "train_ms": train_ms, "us_per_step": 1e3 * train_ms / max(steps, 1),
+            "loss_first": float(hist[0]), "loss_last": float(hist[-1]), "grid": grid,
+            "predict_ms": pred_ms, "predict_wall_ms": 1e3 * wall,
+            "predict_points_per_s": grid * grid / (pred_ms / 1e3)}
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="surrogate network training and prediction speed")
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--grid", type=int, default=2048)
+    ap.add_argument("--seed", type=int, default=1)
+    a = ap.parse_args()
+    print(json.dumps(_speed(a.steps, a.batch, a.grid, a.seed)))

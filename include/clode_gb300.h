@@ -235,6 +235,8 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * "fmad" (0/1: allow contraction of a*b+c; 0 reproduces the reference bit for bit),
  * "prec_div" (1: IEEE division, 0: approximate), "ftz" (1: flush FP32 denormals),
  * "fast_math" (1: approximate exp/log/pow/sin/cos/sqrt, implies prec_div 0 and ftz 1),
+ * "fast_exp" (1: the model's FP32 exp within 2.5 ulp by Cody-Waite splitting and the
+ * hardware exp2; the step-size controller keeps pow),
  * "maxrregcount" (0: no cap, else 32..255 registers per thread),
  * "split_attempts" (adaptive steppers, persistent kernels: 1 = one step attempt per
  * loop iteration, a rejected attempt retried in the next; results are identical),
@@ -242,7 +244,7 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * "fuse_init" (0/1, default 0: run the observer initialisation inside the features
  * launch instead of a launch of its own before it; results are identical),
  * "collect_stats" (0/1).  Read-only for get_option: "last_grid", "last_block".
- * Changing a build option (fmad, prec_div, ftz, fast_math, maxrregcount,
+ * Changing a build option (fmad, prec_div, ftz, fast_math, fast_exp, maxrregcount,
  * split_attempts) recompiles the program at the next run. */
 int clode_sim_set_option(clode_sim *sim, const char *key, double value);
 int clode_sim_get_option(clode_sim *sim, const char *key, double *value);
