@@ -130,17 +130,23 @@ def cpu_sample_indices(n: int, count: int, seed: int) -> np.ndarray:
     return np.sort(rng.choice(n, size=min(count, n), replace=False))
 
 
-def run_cpu(x0, pars, tspan, idx, nthreads: int, prefer_reference: bool = True):
-    """Oracle on the members idx; returns (F rows, seconds, kind)."""
+def run_cpu(x0, pars, tspan, idx, nthreads: int, prefer_reference: bool = True, single: bool = True,
+            tol: float | None = None):
+    """Oracle on the members idx; returns (F rows, seconds, kind).  `single`
+    and `tol` (rtol = abstol) select the precision and tolerance; the default
+    is the workload's own (FP32, 1e-6)."""
     from clode_gb300 import rhs_path
     from oracle.build import OracleConfig, reference_available
     from oracle.runner import OracleSimulator
 
     cfg = OracleConfig(rhs_path("lactotroph.cl"), n_var=N_VAR, n_par=N_PAR, n_aux=N_AUX, stepper="dopri5",
-                       single_precision=True, observer="nhood2", n_store_events=0)
+                       single_precision=single, observer="nhood2", n_store_events=0)
     use_ref = prefer_reference and reference_available()
     s = OracleSimulator(cfg, reference=use_ref, nthreads=nthreads)
-    s.set_solver_params(**SOLVER)
+    sp = dict(SOLVER)
+    if tol is not None:
+        sp.update(abstol=tol, reltol=tol)
+    s.set_solver_params(**sp)
     s.set_observer_params(**{k: v for k, v in OBSERVER.items() if k != "max_event_timestamps"})
     s.set_problem_data(x0[idx], pars[idx])
     s.set_tspan(tspan[idx])
@@ -200,7 +206,8 @@ def bench_surrogate(args, tuned_options: dict) -> dict:
     plain = integrate(P0, P1)
     t_plain = time.perf_counter() - t0
     scr = FeatureMapScreen(integrate, lo=(0.5, 0.0), hi=(3.0, 2.0), n_features=len(SURROGATE_FEATURES), seed=1)
-    res = scr.run(G, G, train_stride=max(G // 512, 1), steps=args.surrogate_steps, batch=args.surrogate_batch,
+    stride = args.surrogate_stride if args.surrogate_stride > 0 else max(G // 512, 1)
+    res = scr.run(G, G, train_stride=stride, steps=args.surrogate_steps, batch=args.surrogate_batch,
                   tol=0.01, keep=0.99, n_calibration=65536, refine=bool(args.surrogate_refine))
     scale = plain.max(axis=0) - plain.min(axis=0)
     err = FeatureMapScreen.map_error(res.features, plain, scale)
@@ -208,7 +215,7 @@ def bench_surrogate(args, tuned_options: dict) -> dict:
     held = rng.choice(G * G, size=min(65536, G * G), replace=False)
     return {
         "workload": f"lactotroph nhood2 map {G}x{G}, tspan [0,3000] ms, features {list(SURROGATE_FEATURES)}",
-        "training": {"steps": args.surrogate_steps, "batch": args.surrogate_batch,
+        "training": {"steps": args.surrogate_steps, "batch": args.surrogate_batch, "stride": stride,
                      "refine": bool(args.surrogate_refine)},
         "error_measure": "max over features of |screened - plain| / feature range over the plain map",
         "points": G * G, "plain_points_per_s": G * G / t_plain, "screened_points_per_s": res.timings["points_per_s"],
@@ -328,6 +335,7 @@ def main():
     ap.add_argument("--surrogate-steps", type=int, default=3000)
     ap.add_argument("--surrogate-batch", type=int, default=4096)
     ap.add_argument("--surrogate-refine", type=int, default=0)
+    ap.add_argument("--surrogate-stride", type=int, default=0, help="training sub-grid stride (0: grid / 512)")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-trajectory", action="store_true")
     ap.add_argument("--trajectory-steps", type=int, default=100000)
@@ -497,6 +505,19 @@ def main():
                                 "event_count_exact_frac": float(np.mean(Fg[:, ev] == Fc[:, ev])),
                                 "mean_period_rel_err_median": float(np.median(rel)),
                                 "mean_period_rel_err_p99": float(np.quantile(rel, 0.99))}
+        # both FP32 results against an FP64 run with a 10^4 tighter tolerance
+        F64, _, _ = run_cpu(x0, pars, tspan, idx, threads, prefer_reference=False, single=False, tol=1e-10)
+
+        def _vs64(Fx):
+            r = np.abs(Fx[:, per] - F64[:, per]) / np.maximum(np.abs(F64[:, per]), 1e-12)
+            return {"event_count_exact_frac": float(np.mean(Fx[:, ev] == F64[:, ev])),
+                    "mean_period_rel_err_median": float(np.median(r)),
+                    "mean_period_rel_err_p99": float(np.quantile(r, 0.99)),
+                    "frac_period_rel_err_above_1e-4": float(np.mean(r > 1e-4)),
+                    "frac_period_rel_err_above_1e-2": float(np.mean(r > 1e-2))}
+
+        line["error_vs_fp64"] = {"reference_run": "CPU oracle, FP64, DP45 rtol = abstol = 1e-10, same members",
+                                 "gpu_fp32": _vs64(Fg), "cpu_fp32": _vs64(Fc)}
     opts = {k: sim.get_option(k) for k in ("schedule", "block_size", "maxrregcount", "fmad", "prec_div", "ftz",
                                            "fast_math", "fast_exp", "split_attempts", "fuse_init")}
     if rank == 0 and not args.no_surrogate:

@@ -7,7 +7,7 @@ feature map from a coarse sub-grid that the ensemble engine integrates.  It
 then predicts the full grid; the cells of the sub-grid where the network
 misses the integrated corners, or where the corners reveal a discontinuity,
 are integrated again by the plain engine, which stays the fallback and the
-judge of the surrogate's error.
+reference for the surrogate's error.
 
 ``FeatureMapScreen.run`` is the whole workflow; ``MLP`` is the network.
 """

@@ -296,7 +296,7 @@ int clode_sim_features_noalloc(clode_sim *sim, long long n_pts, const void *x0, 
                                const void *tspan, unsigned long long *rng, void *dt, void *xf, void *tf,
                                void *F, int *status, void *stream);
 /* Register-file footprint of the built kernels: registers per thread of the features
- * (or transient / trajectory) kernel, as reported by the driver. */
+ * (or transient / trajectory) kernel, as reported by the CUDA driver. */
 int clode_sim_kernel_info(clode_sim *sim, const char *kernel, int *registers, int *max_threads);
 
 /* ------------------------------------- learned surrogate (no reference counterpart) */
