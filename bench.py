@@ -330,7 +330,10 @@ def main():
     ap.add_argument("--fast-exp", type=int, default=0, help="the model's FP32 exp within 2.5 ulp (own Cody-Waite exp)")
     ap.add_argument("--maxrreg", type=int, default=None)
     ap.add_argument("--blocks-per-sm", type=int, default=None)
-    ap.add_argument("--autotune", type=int, default=262144, help="autotune on this many members first (0: off)")
+    ap.add_argument("--split-attempts", type=int, default=None)
+    ap.add_argument("--fuse-init", type=int, default=None)
+    ap.add_argument("--autotune", type=int, default=1048576,
+                    help="autotune on a strided sample of this many members first (0: off)")
     ap.add_argument("--surrogate-grid", type=int, default=4096)
     ap.add_argument("--surrogate-steps", type=int, default=3000)
     ap.add_argument("--surrogate-batch", type=int, default=4096)
@@ -367,7 +370,8 @@ def main():
     sim.set_option("schedule", args.schedule)
     sim.set_option("block_size", args.block_size)
     for key, val in (("prec_div", args.prec_div), ("ftz", args.ftz), ("fast_math", args.fast_math),
-                     ("fast_exp", args.fast_exp),
+                     ("fast_exp", args.fast_exp), ("split_attempts", args.split_attempts),
+                     ("fuse_init", args.fuse_init),
                      ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm)):
         if val is not None:
             sim.set_option(key, val)

@@ -5,6 +5,9 @@ trajectory paths.
 * ``clode_gb300.clode_cpp_wrapper`` — the module clODE's Python package
   imports as ``clode.cpp.clode_cpp_wrapper`` (same classes and names).
 * ``include/clode_gb300.h`` — the C ABI underneath it.
+* ``clode_gb300.surrogate`` — the learned surrogate (tensor-core MLP) and
+  surrogate-screened feature maps.
+* ``clode_gb300.shard`` — splitting an ensemble over several GPUs.
 * ``clode_gb300/rhs/`` — example model sources (clODE's getRHS format).
 """
 import os

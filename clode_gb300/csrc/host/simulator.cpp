@@ -410,10 +410,15 @@ struct clode_sim {
                 kind == CLODE_SIM_FEATURES ? observer.c_str() : "-", single ? "single" : "double");
     }
 
+    // the program was built for the current observer parameters that it compiles in
+    bool observer_program_current() const
+    {
+        return built_nse == op.max_event_timestamps;
+    }
+
     void ensure_built()
     {
-        if (!built || lib == nullptr || lib_device != device ||
-            (kind == CLODE_SIM_FEATURES && built_nse != op.max_event_timestamps)) {
+        if (!built || lib == nullptr || lib_device != device || (kind == CLODE_SIM_FEATURES && !observer_program_current())) {
             if (device_count_or_zero() == 0)
                 fail(CLODE_ERR_NO_DEVICE, "no CUDA device is available (this engine has no CPU path)");
             build();
@@ -774,6 +779,15 @@ struct clode_sim {
         dx.reserve(std::max<size_t>(1, rows * nPts * nVar) * rs);
         aux.reserve(std::max<size_t>(1, rows * nPts * std::max(nAux, 1)) * rs);
         nstored.reserve(std::max<size_t>(1, nPts) * sizeof(int));
+        // rows a run does not reach read as zero after a resize, as in a
+        // freshly created buffer, not as whatever the memory held before
+        ensure_stream();
+        check_cuda(cudaMemsetAsync(t.p, 0, (size_t)rows * nPts * rs, stream), "trajectory clear");
+        check_cuda(cudaMemsetAsync(x.p, 0, (size_t)rows * nPts * nVar * rs, stream), "trajectory clear");
+        check_cuda(cudaMemsetAsync(dx.p, 0, (size_t)rows * nPts * nVar * rs, stream), "trajectory clear");
+        if (nAux > 0)
+            check_cuda(cudaMemsetAsync(aux.p, 0, (size_t)rows * nPts * nAux * rs, stream), "trajectory clear");
+        check_cuda(cudaMemsetAsync(nstored.p, 0, (size_t)nPts * sizeof(int), stream), "trajectory clear");
         traj_rows = rows;
         traj_pts = nPts;
     }
@@ -1656,7 +1670,7 @@ void noalloc_features_prepare(clode_sim *sim, NoallocFeaturesLaunch *out)
         fail(CLODE_ERR_STATE, "not a feature simulator");
     if (!sim->built || !sim->lib || !sim->kp_features)
         fail(CLODE_ERR_NOT_BUILT, "the feature simulator must be built (clode_sim_build) on its device first");
-    if (sim->built_nse != sim->op.max_event_timestamps)
+    if (!sim->observer_program_current())
         fail(CLODE_ERR_NOT_BUILT, "observer parameters changed the program: rebuild with clode_sim_build");
     memset(out, 0, sizeof *out);
     out->kernel = (void *)sim->kp_features;

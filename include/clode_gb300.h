@@ -189,7 +189,9 @@ int clode_sim_set_pars(clode_sim *sim, const double *pars, size_t n);
 int clode_sim_set_tspan(clode_sim *sim, const double *tspan2);
 int clode_sim_set_solver_params(clode_sim *sim, const clode_solver_params *sp);
 int clode_sim_get_solver_params(clode_sim *sim, clode_solver_params *sp);
-int clode_sim_set_observer_params(clode_sim *sim, const clode_observer_params *op); /* CLODEfeatures.cpp:78 */
+/* CLODEfeatures.cpp:78.  max_event_timestamps is compiled into the program: changing it
+ * rebuilds it at the next run (clode_sim_features_noalloc then needs clode_sim_build first). */
+int clode_sim_set_observer_params(clode_sim *sim, const clode_observer_params *op);
 int clode_sim_get_observer_params(clode_sim *sim, clode_observer_params *op);
 /* CLODE::seedRNG() / seedRNG(int) (CLODE.cpp:420-465): use_seed = 0 draws a random seed */
 int clode_sim_seed_rng(clode_sim *sim, int use_seed, int seed);
