@@ -131,6 +131,14 @@ __device__ __forceinline__ void flush_counters(const Args &a, const Counters &c)
 }
 
 // ------------------------------------------------------------ scheduling --
+// Persistent kernels take up to this many steps of a member between the
+// warp-wide votes that refill lanes and detect the end of the launch; a lane
+// whose member ends inside a block waits for the rest of the block.  Per
+// member the steps are exactly those of one step per iteration.
+#ifndef CLODE_STEP_BLOCK
+#define CLODE_STEP_BLOCK 8
+#endif
+
 // Persistent schedule: hand out the next members of [i_begin, i_end) (every
 // i_stride-th one when i_stride > 1, as the autotuner samples) to the lanes of
 // this warp that ask for one, with a single atomic per warp.  Every lane of
@@ -221,11 +229,16 @@ extern "C" __global__ void clode_transient_persistent(const Args a)
             break;
         if (i < 0)
             continue;
-        if (sc.retry || (m.t <= t1 && step < a.sp.max_steps)) {
+        bool running = true;
+        for (int k = 0; k < CLODE_STEP_BLOCK; ++k) {
+            running = sc.retry || (m.t <= t1 && step < a.sp.max_steps);
+            if (!running)
+                break;
             if (!sc.retry)
                 ++step;
             hmin_fail |= step_attempt(m, a.sp, t1, c, sc) == -1;
-        } else {
+        }
+        if (!running) {
             member_store(m, a, i);
             if (a.status)
                 a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, false);
@@ -321,7 +334,11 @@ extern "C" __global__ void clode_trajectory_persistent(const Args a)
             break;
         if (i < 0)
             continue;
-        if (sc.retry || (m.t <= t1 && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store)) {
+        bool running = true;
+        for (int k = 0; k < CLODE_STEP_BLOCK; ++k) {
+            running = sc.retry || (m.t <= t1 && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store);
+            if (!running)
+                break;
             if (!sc.retry)
                 ++step;
             const int flag = step_attempt(m, a.sp, t1, c, sc);
@@ -330,7 +347,8 @@ extern "C" __global__ void clode_trajectory_persistent(const Args a)
                 ++row;
                 store_row(a, m, i, row);
             }
-        } else {
+        }
+        if (!running) {
             a.n_stored[i] = (int)row;
             member_store(m, a, i);
             if (a.status)
@@ -443,13 +461,17 @@ extern "C" __global__ void clode_init_observer_persistent(const Args a)
             t1 = member_t1(a, i);
             fresh = false;
         }
-        const bool running = Observer::two_pass && (sc.retry || (step < a.sp.max_steps && m.t < t1));
-        if (running) {
+        bool running = Observer::two_pass;
+        for (int k = 0; k < CLODE_STEP_BLOCK && running; ++k) {
+            running = sc.retry || (step < a.sp.max_steps && m.t < t1);
+            if (!running)
+                break;
             if (!sc.retry)
                 ++step;
             if (step_attempt(m, a.sp, t1, c, sc) != 1)
                 o.warmup(m.t, m.x, m.dx, m.aux, a.op);
-        } else {
+        }
+        if (!running) {
             if (Observer::two_pass) {
                 // rewind to the initial state (the last noise sample is kept)
                 m.t = member_t0(a, i);
@@ -580,8 +602,11 @@ extern "C" __global__ void clode_features_persistent(const Args a)
             }
             fresh = rewind = false;
         }
-        bool running = sc.retry || (step < a.sp.max_steps && (warm ? m.t < t1 : m.t <= t1));
-        if (running) {
+        bool running = true;
+        for (int k = 0; k < CLODE_STEP_BLOCK && running; ++k) {
+            running = sc.retry || (step < a.sp.max_steps && (warm ? m.t < t1 : m.t <= t1));
+            if (!running)
+                break;
             if (!sc.retry)
                 ++step;
             int flag = step_attempt(m, a.sp, t1, c, sc);
