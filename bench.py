@@ -332,6 +332,7 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=None)
     ap.add_argument("--split-attempts", type=int, default=None)
     ap.add_argument("--fuse-init", type=int, default=None)
+    ap.add_argument("--step-block", type=int, default=None)
     ap.add_argument("--autotune", type=int, default=1048576,
                     help="autotune on a strided sample of this many members first (0: off)")
     ap.add_argument("--surrogate-grid", type=int, default=4096)
@@ -371,7 +372,7 @@ def main():
     sim.set_option("block_size", args.block_size)
     for key, val in (("prec_div", args.prec_div), ("ftz", args.ftz), ("fast_math", args.fast_math),
                      ("fast_exp", args.fast_exp), ("split_attempts", args.split_attempts),
-                     ("fuse_init", args.fuse_init),
+                     ("fuse_init", args.fuse_init), ("step_block", args.step_block),
                      ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm)):
         if val is not None:
             sim.set_option(key, val)

@@ -136,7 +136,7 @@ __device__ __forceinline__ void flush_counters(const Args &a, const Counters &c)
 // whose member ends inside a block waits for the rest of the block.  Per
 // member the steps are exactly those of one step per iteration.
 #ifndef CLODE_STEP_BLOCK
-#define CLODE_STEP_BLOCK 8
+#define CLODE_STEP_BLOCK 16
 #endif
 
 // Persistent schedule: hand out the next members of [i_begin, i_end) (every
@@ -272,11 +272,13 @@ __device__ __forceinline__ void run_trajectory(const Args &a, int i, Counters &c
     unsigned long long row = 0;
     store_row(a, m, i, row);
     unsigned int step = 0;
+    unsigned int to_store = a.sp.nout;  // steps until the next stored row (step % nout == 0)
     bool hmin_fail = false;
     while (m.t <= t1 && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store) {
         ++step;
         hmin_fail |= step_member(m, a.sp, t1, c) != 0;
-        if (step % a.sp.nout == 0) {
+        if (--to_store == 0) {
+            to_store = a.sp.nout;
             ++row;
             store_row(a, m, i, row);
         }
@@ -304,6 +306,7 @@ extern "C" __global__ void clode_trajectory_persistent(const Args a)
     bool exhausted = false;
     int i = -1;
     unsigned int step = 0;
+    unsigned int to_store = 0;  // steps until the next stored row (step % nout == 0)
     unsigned long long row = 0;
     bool hmin_fail = false;
     realtype t1 = ZERO;
@@ -323,6 +326,7 @@ extern "C" __global__ void clode_trajectory_persistent(const Args a)
             } else {
                 i = got;
                 step = 0;
+                to_store = a.sp.nout;
                 row = 0;
                 hmin_fail = false;
                 member_load(m, a, i, c);
@@ -343,7 +347,8 @@ extern "C" __global__ void clode_trajectory_persistent(const Args a)
                 ++step;
             const int flag = step_attempt(m, a.sp, t1, c, sc);
             hmin_fail |= flag == -1;
-            if (flag != 1 && step % a.sp.nout == 0) {
+            if (flag != 1 && --to_store == 0) {
+                to_store = a.sp.nout;
                 ++row;
                 store_row(a, m, i, row);
             }

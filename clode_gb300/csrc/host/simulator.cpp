@@ -221,6 +221,7 @@ struct clode_sim {
     bool fast_math = false;
     bool fast_exp = false;        // FP32 exp and controller pow of a few ulp (CLODE_FAST_EXP)
     bool split_attempts = false;  // persistent kernels: one adaptive attempt per loop iteration
+    int step_block = 16;          // persistent kernels: steps between warp-wide refill votes
     int maxrregcount = 0;
     double time_budget_ms = 0.0;
     bool fuse_init = false;  // separate initialisation launch, as the reference (CLODEfeatures.cpp:180-259)
@@ -345,7 +346,8 @@ struct clode_sim {
                      "-DN_PAR=" + std::to_string(nPar), "-DN_VAR=" + std::to_string(nVar),
                      "-DN_AUX=" + std::to_string(nAux), "-DN_WIENER=" + std::to_string(nWiener),
                      std::string("-DCLODE_SPLIT_ATTEMPTS=") + (split_attempts ? "1" : "0"),
-                     std::string("-DCLODE_FAST_EXP=") + (fast_exp ? "1" : "0")};
+                     std::string("-DCLODE_FAST_EXP=") + (fast_exp ? "1" : "0"),
+                     "-DCLODE_STEP_BLOCK=" + std::to_string(step_block)};
         if (kind == CLODE_SIM_FEATURES) {
             s.defines.push_back("-D" + kObservers.at(observer));
             s.defines.push_back("-DN_STORE_EVENTS=" + std::to_string(op.max_event_timestamps));
@@ -1584,6 +1586,14 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 field = v;
                 sim->built = false;
             }
+        } else if (k == "step_block") {
+            int v = (int)value;
+            if (v < 1 || v > 1024)
+                fail(CLODE_ERR_INVALID_ARGUMENT, "step_block must be in [1, 1024]");
+            if (v != sim->step_block) {
+                sim->step_block = v;
+                sim->built = false;
+            }
         } else if (k == "maxrregcount") {
             int v = (int)value;
             if (v != 0 && (v < 32 || v > 255))
@@ -1619,6 +1629,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "fast_math") *value = sim->fast_math;
         else if (k == "fast_exp") *value = sim->fast_exp;
         else if (k == "split_attempts") *value = sim->split_attempts;
+        else if (k == "step_block") *value = sim->step_block;
         else if (k == "maxrregcount") *value = sim->maxrregcount;
         else if (k == "time_budget_ms") *value = sim->time_budget_ms;
         else if (k == "fuse_init") *value = sim->fuse_init;

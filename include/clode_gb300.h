@@ -242,12 +242,14 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * "maxrregcount" (0: no cap, else 32..255 registers per thread),
  * "split_attempts" (adaptive steppers, persistent kernels: 1 = one step attempt per
  * loop iteration, a rejected attempt retried in the next; results are identical),
+ * "step_block" (persistent kernels: steps taken between the warp-wide votes that
+ * refill lanes, default 16; results are identical),
  * "time_budget_ms" (persistent launches stop taking new members after it),
  * "fuse_init" (0/1, default 0: run the observer initialisation inside the features
  * launch instead of a launch of its own before it; results are identical),
  * "collect_stats" (0/1).  Read-only for get_option: "last_grid", "last_block".
  * Changing a build option (fmad, prec_div, ftz, fast_math, fast_exp, maxrregcount,
- * split_attempts) recompiles the program at the next run. */
+ * split_attempts, step_block) recompiles the program at the next run. */
 int clode_sim_set_option(clode_sim *sim, const char *key, double value);
 int clode_sim_get_option(clode_sim *sim, const char *key, double *value);
 /* Chains: ops run back to back on the simulator's stream, one synchronisation
