@@ -7,12 +7,14 @@
 //                reference's NDRange(nPts) launch (clode/cpp/CLODE.cpp:484).
 //  * persistent: a fixed grid (a multiple of the SM count) whose lanes pull
 //                members from a global counter one at a time.  A lane whose
-//                member finishes early refills itself immediately, so
-//                members of very different lengths (adaptive steps,
-//                per-member time spans, terminal events, two-pass observers)
-//                keep every lane busy.  Both passes of a two-pass observer
-//                run through the same stepper call, so lanes in different
-//                passes stay converged on the expensive part of the loop.
+//                member finishes early refills itself at the next warp-wide
+//                vote (every CLODE_STEP_BLOCK steps), so members of very
+//                different lengths (adaptive steps, per-member time spans,
+//                terminal events, two-pass observers) keep every lane busy.
+//                A two-pass observer's warm-up pass runs as its own launch
+//                (clode_init_observer_persistent) or, fused, inside the
+//                features launch through the same stepper call as the
+//                feature pass.
 //
 // Per member, both schedules execute the same arithmetic in the same order,
 // so their results are identical.  Member semantics follow
