@@ -273,13 +273,59 @@ def bench_trajectory(args, tuned_options: dict) -> dict:
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     gbs = written / (ms / 1e3) / 1e9
-    return {"workload": f"OU trajectories, 65536 members (256 parameter points x 256 realisations), seuler "
+    frontend = bench_trajectory_frontend(W, pi, pars, tuned_options, args) if args.trajectory_frontend else None
+    return {"frontend": frontend,
+            "workload": f"OU trajectories, 65536 members (256 parameter points x 256 realisations), seuler "
                         f"dt 1e-3 over [0, {steps * 1e-3:g}], (t, x, dx) stored every 10 steps, FP32",
             "members": n, "steps_per_member": steps, "rows": rows, "ms": ms, "ms_all": times,
             "member_steps_per_s": n * steps / (ms / 1e3),
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
                          "traffic": None, "algorithmic_bytes": written,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"}}
+
+
+def bench_trajectory_frontend(W, pi, pars, tuned_options: dict, args) -> dict:
+    """Per-member trajectory outputs on the host, the step after the
+    trajectory kernel: clode_gb300.trajectory_output.get_trajectory (device
+    regrouping, one copy per array, views) against the restatement of
+    clODE's getters plus per-member loop (clode/trajectory.py:216-264) as the
+    CPU baseline, on the first 8,192 members of the OU workload (32 parameter
+    points x 256 realisations) over 20,000 steps: 2,001 rows of (t, x, dx)
+    per member, 393 MB as float64."""
+    from clode_gb300.trajectory_output import get_trajectory
+    from oracle.trajectory_frontend import reference_get_trajectory
+
+    n, steps, nout = 8192, 20000, 10
+    sim = W.TrajectorySimulatorBase(pi, "seuler", True, W.OpenCLResource(), "")
+    for k in ("schedule", "block_size", "fmad", "prec_div", "ftz"):
+        if k in tuned_options:
+            sim.set_option(k, tuned_options[k])
+    sim.build_cl()
+    sim.set_solver_params(W.SolverParams(dt=1e-3, dtmax=1.0, abstol=1e-6, reltol=1e-3, max_steps=steps,
+                                         max_store=steps // nout + 2, nout=nout))
+    sim.set_problem_data(np.zeros(n), pars[:n].flatten(order="F"))
+    sim.set_tspan([0.0, steps * 1e-3])
+    sim.seed_rng(args.seed)
+    sim.trajectory()
+    ours, ref = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        out = get_trajectory(sim)
+        ours.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        want = reference_get_trajectory(sim, ["x"], [], n, steps // nout + 2)
+        ref.append(time.perf_counter() - t0)
+    same = all(np.array_equal(o.t, w["t"]) and np.array_equal(o.x, w["x"]) and np.array_equal(o.dx, w["dx"])
+               for o, w in zip(out, want))
+    rows = int(np.asarray(sim.get_n_stored()).max()) + 1
+    nbytes = n * rows * 3 * 8
+    return {"workload": f"per-member outputs of {n} OU trajectories x {rows} rows of (t, x, dx), float64",
+            "members": n, "rows": rows, "bytes": nbytes, "s": min(ours), "gb_per_s": nbytes / min(ours) / 1e9,
+            "identical_to_baseline": bool(same),
+            "cpu_baseline": {"s": min(ref), "kind": "port", "cores": 1,
+                             "sample": "clODE's getters + per-member loop (clode/trajectory.py:216-264), "
+                                       "restated, over the same device arrays"},
+            "speedup": min(ref) / min(ours)}
 
 
 def bench_reference_arm(args):
@@ -343,6 +389,8 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-trajectory", action="store_true")
     ap.add_argument("--trajectory-steps", type=int, default=100000)
+    ap.add_argument("--trajectory-frontend", type=int, default=1,
+                    help="1: also time per-member trajectory outputs against clODE's per-member loop")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
 

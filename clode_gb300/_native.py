@@ -24,6 +24,7 @@ ERROR_NAMES = {
 SIM_BASE, SIM_FEATURES, SIM_TRAJECTORY = 0, 1, 2
 ARRAY_X0, ARRAY_XF, ARRAY_DT, ARRAY_TF, ARRAY_PARS, ARRAY_TSPAN = 0, 1, 2, 3, 4, 5
 ARRAY_F, ARRAY_T, ARRAY_X, ARRAY_DX, ARRAY_AUX = 6, 7, 8, 9, 10
+ARRAY_EVENT_T, ARRAY_EVENT_X, ARRAY_EVENT_DX, ARRAY_EVENT_AUX = 11, 12, 13, 14
 STRING_PROGRAM, STRING_FEATURE_NAMES, STRING_AVAILABLE_STEPPERS = 0, 1, 2
 STRING_AVAILABLE_OBSERVERS, STRING_OBSERVER_NAME, STRING_STEPPER = 3, 4, 5
 STRING_STATUS_REPORT, STRING_BUILD_LOG = 6, 7
@@ -65,7 +66,8 @@ class CDeviceInfo(C.Structure):
 
 class CSizes(C.Structure):
     _fields_ = [(n, C.c_longlong) for n in ("n_pts", "n_var", "n_par", "n_aux", "n_wiener", "n_features",
-                                             "max_store", "t_elements", "x_elements", "aux_elements")]
+                                             "max_store", "t_elements", "x_elements", "aux_elements",
+                                             "n_store_var", "n_store_aux", "event_rows")]
 
 
 LOG_SINK = C.CFUNCTYPE(None, C.c_int, C.c_char_p)
@@ -117,6 +119,11 @@ SIGNATURES = {
     "clode_sim_get_string": (C.c_int, [_P, C.c_int, C.c_char_p, _SIZE, C.POINTER(_SIZE)]),
     "clode_sim_set_tspan_per_member": (C.c_int, [_P, _DP, _SIZE]),
     "clode_sim_get_status": (C.c_int, [_P, C.POINTER(C.c_int), _SIZE, C.POINTER(_SIZE)]),
+    "clode_sim_features_store": (C.c_int, [_P, C.c_int, C.c_uint]),
+    "clode_sim_get_n_events": (C.c_int, [_P, C.POINTER(C.c_int), _SIZE, C.POINTER(_SIZE)]),
+    "clode_sim_set_store_variables": (C.c_int, [_P, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int]),
+    "clode_sim_get_trajectory_by_member": (C.c_int, [_P, C.c_longlong, C.c_longlong, C.c_longlong, _DP, _DP, _DP,
+                                                     _DP, C.POINTER(C.c_int)]),
     "clode_sim_get_rng_state": (C.c_int, [_P, C.POINTER(C.c_ulonglong), _SIZE, C.POINTER(_SIZE)]),
     "clode_sim_set_rng_state": (C.c_int, [_P, C.POINTER(C.c_ulonglong), _SIZE]),
     "clode_sim_get_stats": (C.c_int, [_P, C.POINTER(C.c_ulonglong)]),

@@ -655,8 +655,84 @@ class SimulatorBase:
     def get_build_log(self) -> str:
         return self._get_string(N.STRING_BUILD_LOG)
 
+    def set_store_variables(self, var_ix: Optional[List[int]] = None, aux_ix: Optional[List[int]] = None) -> None:
+        """Store only these variables (and auxiliary variables) in trajectory
+        rows and event states, in the given order; None keeps all of them.
+        Addition (clode/cpp/trajectory.cl:3 leaves it as a TODO); the getters
+        then return ``len(var_ix)`` (``len(aux_ix)``) columns per row."""
+        def arr(ix):
+            if ix is None:
+                return None, -1
+            a = (C.c_int * max(1, len(ix)))(*[int(v) for v in ix])
+            return a, len(ix)
+        v, nv = arr(var_ix)
+        w, nw = arr(aux_ix)
+        _check(N.lib.clode_sim_set_store_variables(self._handle, v, nv, w, nw))
 
-class FeatureSimulatorBase(SimulatorBase):
+
+class _StoredRows:
+    """Getters of stored trajectory rows, shared by TrajectorySimulatorBase
+    (clode/cpp/CLODEtrajectory.hpp:37-48) and the features-with-storage runs
+    of FeatureSimulatorBase."""
+
+    def get_t(self) -> np.ndarray:
+        return self._get(N.ARRAY_T)
+
+    def get_x(self) -> np.ndarray:
+        return self._get(N.ARRAY_X)
+
+    def get_dx(self) -> np.ndarray:
+        return self._get(N.ARRAY_DX)
+
+    def get_aux(self) -> np.ndarray:
+        return self._get(N.ARRAY_AUX)
+
+    def get_n_stored(self) -> np.ndarray:
+        n = C.c_size_t(0)
+        _check(N.lib.clode_sim_get_n_stored(self._handle, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.int32)
+        if n.value:
+            _check(N.lib.clode_sim_get_n_stored(self._handle, out.ctypes.data_as(C.POINTER(C.c_int)), out.size,
+                                                C.byref(n)))
+        return out
+
+    def get_trajectory_by_member(self, first: int = 0, count: Optional[int] = None, rows: Optional[int] = None,
+                                 which=("t", "x", "dx", "aux")) -> dict:
+        """The last trajectory regrouped by member on the device (addition).
+
+        Returns ``{"n_stored": (count,), "t": (count, rows), "x": (count, rows,
+        nVar), "dx": (count, rows, nVar), "aux": (count, rows, nAux)}`` float64
+        arrays for members ``first .. first + count - 1``: member i's rows
+        are ``t[i, :n_stored[i] + 1]`` etc., the slices clODE's
+        ``TrajectorySimulator.get_trajectory`` builds one member at a time
+        (clode/trajectory.py:216-264).  ``rows`` defaults to the longest
+        stored trajectory among those members; ``which`` selects the arrays
+        to fetch ("aux" is omitted when the model has none).
+        """
+        s = N.CSizes()
+        _check(N.lib.clode_sim_get_sizes(self._handle, C.byref(s)))
+        n_pts, n_var, n_aux = int(s.n_pts), int(s.n_store_var), int(s.n_store_aux)
+        count = n_pts - first if count is None else int(count)
+        ns = np.zeros(max(count, 0), dtype=np.int32)
+        _check(N.lib.clode_sim_get_trajectory_by_member(self._handle, first, count, 0, None, None, None, None,
+                                                         ns.ctypes.data_as(C.POINTER(C.c_int))))
+        if rows is None:
+            rows = min(int(s.max_store), int(ns.max()) + 1) if count > 0 else 0
+        out = {"n_stored": ns}
+        shapes = {"t": (count, rows), "x": (count, rows, n_var), "dx": (count, rows, n_var),
+                  "aux": (count, rows, n_aux)}
+        ptrs = []
+        for k in ("t", "x", "dx", "aux"):
+            if k in which and not (k == "aux" and n_aux == 0):
+                out[k] = np.empty(shapes[k], dtype=np.float64)
+                ptrs.append(N.dptr(out[k]))
+            else:
+                ptrs.append(None)
+        _check(N.lib.clode_sim_get_trajectory_by_member(self._handle, first, count, rows, *ptrs, None))
+        return out
+
+
+class FeatureSimulatorBase(SimulatorBase, _StoredRows):
     """clODE's CLODEfeatures class (clode/cpp/CLODEfeatures.hpp:23-76)."""
 
     _kind = N.SIM_FEATURES
@@ -691,6 +767,38 @@ class FeatureSimulatorBase(SimulatorBase):
         flag = -1 if reinitialize_observer is None else int(bool(reinitialize_observer))
         _check(N.lib.clode_sim_features(self._handle, flag))
 
+    def features_store(self, reinitialize_observer: Optional[bool] = None, event_rows: int = 0) -> None:
+        """features() that also stores, in the same pass, the trajectory rows
+        (as TrajectorySimulatorBase.trajectory: row 0 and every nout-th step,
+        read with get_t/get_x/get_dx/get_aux/get_n_stored) and the state at
+        each of the first ``event_rows`` observer events (get_event_t/x/dx/aux,
+        get_n_events).  Addition: the design of the reference's unused unified
+        driver (clode/cpp/odedriver.cl:10-162), repaired; F, xf, dt, tf and
+        the RNG state come out as from features()."""
+        flag = -1 if reinitialize_observer is None else int(bool(reinitialize_observer))
+        _check(N.lib.clode_sim_features_store(self._handle, flag, int(event_rows)))
+
+    def get_event_t(self) -> np.ndarray:
+        return self._get(N.ARRAY_EVENT_T)
+
+    def get_event_x(self) -> np.ndarray:
+        return self._get(N.ARRAY_EVENT_X)
+
+    def get_event_dx(self) -> np.ndarray:
+        return self._get(N.ARRAY_EVENT_DX)
+
+    def get_event_aux(self) -> np.ndarray:
+        return self._get(N.ARRAY_EVENT_AUX)
+
+    def get_n_events(self) -> np.ndarray:
+        n = C.c_size_t(0)
+        _check(N.lib.clode_sim_get_n_events(self._handle, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.int32)
+        if n.value:
+            _check(N.lib.clode_sim_get_n_events(self._handle, out.ctypes.data_as(C.POINTER(C.c_int)), out.size,
+                                                C.byref(n)))
+        return out
+
     def get_observer_params(self) -> ObserverParams:
         c = N.CObserverParams()
         _check(N.lib.clode_sim_get_observer_params(self._handle, C.byref(c)))
@@ -715,7 +823,7 @@ class FeatureSimulatorBase(SimulatorBase):
         return self._get_string(N.STRING_AVAILABLE_OBSERVERS).split("\n")
 
 
-class TrajectorySimulatorBase(SimulatorBase):
+class TrajectorySimulatorBase(SimulatorBase, _StoredRows):
     """clODE's CLODEtrajectory class (clode/cpp/CLODEtrajectory.hpp:21-52)."""
 
     _kind = N.SIM_TRAJECTORY
@@ -729,24 +837,3 @@ class TrajectorySimulatorBase(SimulatorBase):
 
     def trajectory(self) -> None:
         _check(N.lib.clode_sim_trajectory(self._handle))
-
-    def get_t(self) -> np.ndarray:
-        return self._get(N.ARRAY_T)
-
-    def get_x(self) -> np.ndarray:
-        return self._get(N.ARRAY_X)
-
-    def get_dx(self) -> np.ndarray:
-        return self._get(N.ARRAY_DX)
-
-    def get_aux(self) -> np.ndarray:
-        return self._get(N.ARRAY_AUX)
-
-    def get_n_stored(self) -> np.ndarray:
-        n = C.c_size_t(0)
-        _check(N.lib.clode_sim_get_n_stored(self._handle, None, 0, C.byref(n)))
-        out = np.zeros(n.value, dtype=np.int32)
-        if n.value:
-            _check(N.lib.clode_sim_get_n_stored(self._handle, out.ctypes.data_as(C.POINTER(C.c_int)), out.size,
-                                                C.byref(n)))
-        return out

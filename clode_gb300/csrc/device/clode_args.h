@@ -83,6 +83,15 @@ struct ArgsT {
     R *dx_out;
     R *aux_out;
     int *n_stored;
+    // features with storage (programs built with CLODE_FEATURE_STORE): the
+    // state at each of the first ev_rows observer events of a member,
+    // [k * nPts * n + j * nPts + i], and the member's event count
+    R *ev_t;
+    R *ev_x;
+    R *ev_dx;
+    R *ev_aux;
+    int *n_events;
+    unsigned int ev_rows;
     // optional diagnostics (may be null)
     int *status;
     unsigned long long *stats;

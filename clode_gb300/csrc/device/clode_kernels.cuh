@@ -22,6 +22,10 @@
 // and trajectory.cl:14-112.
 #pragma once
 
+#ifndef CLODE_FEATURE_STORE
+#define CLODE_FEATURE_STORE 0
+#endif
+
 namespace clode {
 
 typedef ArgsT<realtype> Args;
@@ -251,19 +255,45 @@ extern "C" __global__ void clode_transient_persistent(const Args a)
 }
 
 // ------------------------------------------------------------ trajectory --
+// Stored columns: every variable and auxiliary variable, or the subsets
+// compiled in as index lists CLODE_STORE_VARS / CLODE_STORE_AUX of lengths
+// CLODE_STORE_NV / CLODE_STORE_NA (the option clode/cpp/trajectory.cl:3
+// leaves as a TODO: "store only a subset of variables (allow bigger nPts)").
+// A row is t, the stored x, the stored dx (same indices) and the stored aux.
+#ifdef CLODE_STORE_NV
+__device__ constexpr int clode_store_var_ix[CLODE_STORE_NV > 0 ? CLODE_STORE_NV : 1] = {CLODE_STORE_VARS};
+#define CLODE_STORE_VAR(k) clode_store_var_ix[k]
+#else
+#define CLODE_STORE_NV N_VAR
+#define CLODE_STORE_VAR(k) (k)
+#endif
+#ifdef CLODE_STORE_NA
+__device__ constexpr int clode_store_aux_ix[CLODE_STORE_NA > 0 ? CLODE_STORE_NA : 1] = {CLODE_STORE_AUX};
+#define CLODE_STORE_AUXV(k) clode_store_aux_ix[k]
+#else
+#define CLODE_STORE_NA N_AUX
+#define CLODE_STORE_AUXV(k) (k)
+#endif
+
+// rows [row * nPts * w + k * nPts + i] (trajectory.cl:63-71, :83-95)
+__device__ __forceinline__ void store_state(realtype *t, realtype *x, realtype *dx, realtype *aux,
+                                            unsigned long long n, int i, unsigned long long row, const Member &m)
+{
+    t[row * n + i] = m.t;
+#pragma unroll
+    for (int k = 0; k < CLODE_STORE_NV; ++k)
+        x[(row * CLODE_STORE_NV + k) * n + i] = m.x[CLODE_STORE_VAR(k)];
+#pragma unroll
+    for (int k = 0; k < CLODE_STORE_NV; ++k)
+        dx[(row * CLODE_STORE_NV + k) * n + i] = m.dx[CLODE_STORE_VAR(k)];
+#pragma unroll
+    for (int k = 0; k < CLODE_STORE_NA; ++k)
+        aux[(row * CLODE_STORE_NA + k) * n + i] = m.aux[CLODE_STORE_AUXV(k)];
+}
+
 __device__ __forceinline__ void store_row(const Args &a, const Member &m, int i, unsigned long long row)
 {
-    const unsigned long long n = (unsigned long long)a.nPts;
-    a.t_out[row * n + i] = m.t;
-#pragma unroll
-    for (int j = 0; j < N_VAR; ++j)
-        a.x_out[row * n * N_VAR + j * n + i] = m.x[j];
-#pragma unroll
-    for (int j = 0; j < N_VAR; ++j)
-        a.dx_out[row * n * N_VAR + j * n + i] = m.dx[j];
-#pragma unroll
-    for (int j = 0; j < N_AUX; ++j)
-        a.aux_out[row * n * N_AUX + j * n + i] = m.aux[j];
+    store_state(a.t_out, a.x_out, a.dx_out, a.aux_out, (unsigned long long)a.nPts, i, row, m);
 }
 
 __device__ __forceinline__ void run_trajectory(const Args &a, int i, Counters &c)
@@ -494,6 +524,52 @@ extern "C" __global__ void clode_init_observer_persistent(const Args a)
     flush_counters(a, c);
 }
 
+#if CLODE_FEATURE_STORE
+// Features with storage: the feature pass also stores the trajectory rows
+// (row 0 at the start, then every nout-th step, at most max_store + 1 rows,
+// as trajectory.cl:63-95) and the state at each of the first ev_rows
+// observer events.  This is the design of the reference's unused unified
+// driver (clode/cpp/odedriver.cl:10-162, and the "record current state into
+// dedicated event buffers" note at features.cl:76), with its defects
+// repaired: events are numbered from 0, and a full trajectory buffer stops
+// the storing but not the integration, so the features, final state and RNG
+// state are those of the features kernel.
+struct FeatureStore {
+    unsigned long long row;
+    unsigned int to_store;  // steps until the next stored row (step % nout == 0)
+    unsigned int ev;
+
+    __device__ __forceinline__ void start(const Args &a, const Member &m, int i)
+    {
+        row = 0;
+        to_store = a.sp.nout;
+        ev = 0;
+        store_row(a, m, i, 0);
+    }
+    __device__ __forceinline__ void after_step(const Args &a, const Member &m, int i)
+    {
+        if (--to_store == 0) {
+            to_store = a.sp.nout;
+            if (row < (unsigned long long)a.sp.max_store) {
+                ++row;
+                store_row(a, m, i, row);
+            }
+        }
+    }
+    __device__ __forceinline__ void on_event(const Args &a, const Member &m, int i)
+    {
+        if (ev < a.ev_rows)
+            store_state(a.ev_t, a.ev_x, a.ev_dx, a.ev_aux, (unsigned long long)a.nPts, i, ev, m);
+        ++ev;
+    }
+    __device__ __forceinline__ void finish(const Args &a, int i) const
+    {
+        a.n_stored[i] = (int)row;
+        a.n_events[i] = (int)ev;
+    }
+};
+#endif
+
 // Feature pass for one member (features.cl:10-106)
 __device__ __forceinline__ void features_member(Observer &o, const Args &a, int i, Counters &c)
 {
@@ -503,18 +579,31 @@ __device__ __forceinline__ void features_member(Observer &o, const Args &a, int 
     const realtype t1 = member_t1(a, i);
     unsigned int step = 0;
     bool hmin_fail = false, terminal = false;
+#if CLODE_FEATURE_STORE
+    FeatureStore fs;
+    fs.start(a, m, i);
+#endif
     while (m.t <= t1 && step < a.sp.max_steps) {
         ++step;
         hmin_fail |= step_member(m, a.sp, t1, c) != 0;
+#if CLODE_FEATURE_STORE
+        fs.after_step(a, m, i);
+#endif
         o.update(m.t, m.x, m.dx, m.aux, a.op);
         if (o.event(m.t, m.x, m.dx, m.aux, a.op)) {
             c.events++;
+#if CLODE_FEATURE_STORE
+            fs.on_event(a, m, i);
+#endif
             if (o.on_event(m.t, m.x, m.dx, m.aux, a.op)) {
                 terminal = true;
                 break;
             }
         }
     }
+#if CLODE_FEATURE_STORE
+    fs.finish(a, i);
+#endif
     FOut out = {a.F, (unsigned long long)a.nPts, i, 0};
     o.write(out);
     o.rebase(m.t - t0);
@@ -562,6 +651,9 @@ extern "C" __global__ void clode_features_persistent(const Args a)
     Observer o;
     StepCtl sc;
     sc.retry = false;
+#if CLODE_FEATURE_STORE
+    FeatureStore fs;
+#endif
     for (;;) {
         bool want = i < 0 && !exhausted;
         if (want && budget_spent(a, t_start)) {
@@ -608,6 +700,10 @@ extern "C" __global__ void clode_features_persistent(const Args a)
                 warm = false;
             }
             fresh = rewind = false;
+#if CLODE_FEATURE_STORE
+            if (!warm)  // the feature pass starts here
+                fs.start(a, m, i);
+#endif
         }
         bool running = true;
         for (int k = 0; k < CLODE_STEP_BLOCK && running; ++k) {
@@ -623,9 +719,15 @@ extern "C" __global__ void clode_features_persistent(const Args a)
                 o.warmup(m.t, m.x, m.dx, m.aux, a.op);
             } else {
                 hmin_fail |= flag != 0;
+#if CLODE_FEATURE_STORE
+                fs.after_step(a, m, i);
+#endif
                 o.update(m.t, m.x, m.dx, m.aux, a.op);
                 if (o.event(m.t, m.x, m.dx, m.aux, a.op)) {
                     c.events++;
+#if CLODE_FEATURE_STORE
+                    fs.on_event(a, m, i);
+#endif
                     if (o.on_event(m.t, m.x, m.dx, m.aux, a.op)) {
                         terminal = true;
                         running = false;
@@ -637,6 +739,9 @@ extern "C" __global__ void clode_features_persistent(const Args a)
             if (warm) {
                 rewind = true;
             } else {
+#if CLODE_FEATURE_STORE
+                fs.finish(a, i);
+#endif
                 FOut out = {a.F, (unsigned long long)a.nPts, i, 0};
                 o.write(out);
                 o.rebase(m.t - t0);

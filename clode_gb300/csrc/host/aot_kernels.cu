@@ -60,7 +60,69 @@ __global__ void k_fill(T *dst, T v, size_t n)
         dst[i] = v;
 }
 
+// Trajectory rows regrouped by member.  The trajectory kernel stores row r,
+// column j of member i at [(r * width + j) * ld + i] (members fastest, so its
+// stores coalesce); clODE's TrajectorySimulator.get_trajectory slices every
+// member's rows out of that on the host (clode/trajectory.py:216-264).  This
+// is the transpose of the (rows * width) x members matrix into member-major
+// doubles, dst[(i - m0) * nc + c]: 32 x 32 tiles staged through shared
+// memory, loads coalesced along members, stores along c, every element read
+// once and written once.  Tiles are walked grid-stride so any number of rows
+// fits one launch.
+constexpr int kTile = 32, kTileRows = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(kTile *kTileRows)
+    k_regroup_by_member(const T *__restrict__ src, size_t ld, size_t m0, size_t nm, size_t nc,
+                        double *__restrict__ dst)
+{
+    __shared__ double tile[kTile][kTile + 1];
+    const size_t tiles_m = (nm + kTile - 1) / kTile;
+    const size_t tiles = tiles_m * ((nc + kTile - 1) / kTile);
+    for (size_t b = blockIdx.x; b < tiles; b += gridDim.x) {
+        const size_t i0 = (b % tiles_m) * kTile, c0 = (b / tiles_m) * kTile;
+        const size_t i = i0 + threadIdx.x;
+        for (int k = threadIdx.y; k < kTile; k += kTileRows) {
+            const size_t c = c0 + k;
+            if (c < nc && i < nm)
+                tile[k][threadIdx.x] = (double)src[c * ld + m0 + i];
+        }
+        __syncthreads();
+        const size_t c = c0 + threadIdx.x;
+        for (int k = threadIdx.y; k < kTile; k += kTileRows) {
+            const size_t ii = i0 + k;
+            if (c < nc && ii < nm)
+                dst[ii * nc + c] = tile[threadIdx.x][k];
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+void launch_regroup(const T *src, size_t ld, size_t m0, size_t nm, size_t nc, double *dst, cudaStream_t s)
+{
+    if (!nm || !nc) return;
+    const size_t tiles = ((nm + kTile - 1) / kTile) * ((nc + kTile - 1) / kTile);
+    // 152 SMs x 8 resident 256-thread blocks; more tiles are walked grid-stride
+    const unsigned int grid = (unsigned int)std::min<size_t>(tiles, 152 * 8);
+    k_regroup_by_member<T><<<grid, dim3(kTile, kTileRows), 0, s>>>(src, ld, m0, nm, nc, dst);
+    count_launch();
+    check_cuda(cudaGetLastError(), "trajectory regroup launch");
+}
+
 }  // namespace
+
+void launch_regroup_by_member_f32(const float *src, size_t ld, size_t m0, size_t nm, size_t nc, double *dst,
+                                  cudaStream_t s)
+{
+    launch_regroup<float>(src, ld, m0, nm, nc, dst, s);
+}
+
+void launch_regroup_by_member_f64(const double *src, size_t ld, size_t m0, size_t nm, size_t nc, double *dst,
+                                  cudaStream_t s)
+{
+    launch_regroup<double>(src, ld, m0, nm, nc, dst, s);
+}
 
 void launch_f64_to_f32(const double *src, float *dst, size_t n, cudaStream_t s)
 {

@@ -190,6 +190,7 @@ struct clode_sim {
     int buffers_device = -1;
     bool buffers_single = true;
     DevBuf x0, pars, xf, rng, dt, tf, tspan_dev, odata, F, t, x, dx, aux, nstored, status, stats, stage, work;
+    DevBuf ev_t, ev_x, ev_dx, ev_aux, nevents;  // features with storage: event states
 
     // program
     bool built = false;
@@ -209,7 +210,16 @@ struct clode_sim {
     unsigned int odata_words_alloc = 0;
     bool observer_initialized = false;
     // trajectory bookkeeping (CLODEtrajectory.cpp:45-94)
-    long long traj_rows = -1, traj_pts = -1;
+    long long traj_rows = -1, traj_pts = -1, traj_width = -1;
+    // stored columns (all when store_subset is false) and the event store
+    bool store_subset = false;
+    std::vector<int> store_var_ix, store_aux_ix;
+    bool want_store = false;  // build the features kernels with storage (CLODE_FEATURE_STORE)
+    bool built_store = false;
+    std::string built_subset;
+    long long ev_rows_alloc = -1, ev_pts = -1, ev_width = -1;
+    unsigned int ev_rows = 0;
+    bool events_valid = false;
 
     // engine options
     int schedule = 0;
@@ -255,7 +265,9 @@ struct clode_sim {
 
     std::vector<DevBuf *> all_buffers()
     {
-        return {&x0, &pars, &xf, &rng, &dt, &tf, &tspan_dev, &odata, &F, &t, &x, &dx, &aux, &nstored, &status, &stats, &stage, &work};
+        return {&x0,  &pars,   &xf,    &rng,    &dt,   &tf,    &tspan_dev, &odata, &F,
+                &t,   &x,      &dx,    &aux,    &nstored, &status, &stats, &stage, &work,
+                &ev_t, &ev_x, &ev_dx, &ev_aux, &nevents};
     }
 
     size_t real_size() const { return single ? sizeof(float) : sizeof(double); }
@@ -285,7 +297,47 @@ struct clode_sim {
             aux_names.push_back("aux" + std::to_string(aux_names.size()));
         var_names.resize(nVar);
         aux_names.resize(nAux);
+        store_subset = false;  // stored columns index the old problem's variables
+        store_var_ix.clear();
+        store_aux_ix.clear();
         built = false;
+    }
+
+    // Stored columns of trajectories and event states.  A negative count
+    // keeps every variable (or auxiliary variable); both negative restore
+    // the reference layout.  Invalidates the stored arrays of earlier runs.
+    void set_store_variables(const int *var_ix, int n_var_ix, const int *aux_ix, int n_aux_ix)
+    {
+        std::vector<int> v, w;
+        if (n_var_ix >= 0) {
+            if (n_var_ix > 0 && !var_ix)
+                fail(CLODE_ERR_INVALID_ARGUMENT, "variable index list is null");
+            for (int k = 0; k < n_var_ix; ++k) {
+                if (var_ix[k] < 0 || var_ix[k] >= nVar)
+                    fail(CLODE_ERR_INVALID_ARGUMENT, "stored variable index %d is outside [0, %d)", var_ix[k], nVar);
+                v.push_back(var_ix[k]);
+            }
+        } else {
+            for (int k = 0; k < nVar; ++k)
+                v.push_back(k);
+        }
+        if (n_aux_ix >= 0) {
+            if (n_aux_ix > 0 && !aux_ix)
+                fail(CLODE_ERR_INVALID_ARGUMENT, "auxiliary index list is null");
+            for (int k = 0; k < n_aux_ix; ++k) {
+                if (aux_ix[k] < 0 || aux_ix[k] >= nAux)
+                    fail(CLODE_ERR_INVALID_ARGUMENT, "stored auxiliary index %d is outside [0, %d)", aux_ix[k], nAux);
+                w.push_back(aux_ix[k]);
+            }
+        } else {
+            for (int k = 0; k < nAux; ++k)
+                w.push_back(k);
+        }
+        store_subset = n_var_ix >= 0 || n_aux_ix >= 0;
+        store_var_ix = store_subset ? v : std::vector<int>();
+        store_aux_ix = store_subset ? w : std::vector<int>();
+        traj_rows = -1;
+        events_valid = false;
     }
 
     void set_stepper(const char *s)
@@ -331,6 +383,23 @@ struct clode_sim {
     }
 
     // ------------------------------------------------------------ build --
+    static std::string join_ix(const std::vector<int> &v)
+    {
+        std::string r;
+        for (size_t k = 0; k < v.size(); ++k)
+            r += (k ? "," : "") + std::to_string(v[k]);
+        return r;
+    }
+
+    std::string subset_key() const
+    {
+        return store_subset ? join_ix(store_var_ix) + "/" + join_ix(store_aux_ix) : std::string("all");
+    }
+
+    // stored columns per row: x (and dx) and aux
+    int store_nv() const { return store_subset ? (int)store_var_ix.size() : nVar; }
+    int store_na() const { return store_subset ? (int)store_aux_ix.size() : nAux; }
+
     ProgramSpec spec() const
     {
         ProgramSpec s;
@@ -351,8 +420,16 @@ struct clode_sim {
         if (kind == CLODE_SIM_FEATURES) {
             s.defines.push_back("-D" + kObservers.at(observer));
             s.defines.push_back("-DN_STORE_EVENTS=" + std::to_string(op.max_event_timestamps));
+            if (want_store)
+                s.defines.push_back("-DCLODE_FEATURE_STORE=1");
         } else {
             s.defines.push_back("-DN_STORE_EVENTS=0");
+        }
+        if (store_subset) {
+            s.defines.push_back("-DCLODE_STORE_NV=" + std::to_string(store_var_ix.size()));
+            s.defines.push_back("-DCLODE_STORE_VARS=" + join_ix(store_var_ix));
+            s.defines.push_back("-DCLODE_STORE_NA=" + std::to_string(store_aux_ix.size()));
+            s.defines.push_back("-DCLODE_STORE_AUX=" + join_ix(store_aux_ix));
         }
         return s;
     }
@@ -407,6 +484,8 @@ struct clode_sim {
         prog = p;
         built_key = p.key;
         built_nse = op.max_event_timestamps;
+        built_store = want_store;
+        built_subset = subset_key();
         built = true;
         log_msg(CLODE_LOG_DEBUG, "program %s ready (%s, %s, %s)", p.key.c_str(), stepper.c_str(),
                 kind == CLODE_SIM_FEATURES ? observer.c_str() : "-", single ? "single" : "double");
@@ -420,7 +499,8 @@ struct clode_sim {
 
     void ensure_built()
     {
-        if (!built || lib == nullptr || lib_device != device || (kind == CLODE_SIM_FEATURES && !observer_program_current())) {
+        if (!built || lib == nullptr || lib_device != device || (kind == CLODE_SIM_FEATURES && !observer_program_current()) ||
+            built_store != want_store || built_subset != subset_key()) {
             if (device_count_or_zero() == 0)
                 fail(CLODE_ERR_NO_DEVICE, "no CUDA device is available (this engine has no CPU path)");
             build();
@@ -585,6 +665,12 @@ struct clode_sim {
         a.dx_out = dx.as<R>();
         a.aux_out = aux.as<R>();
         a.n_stored = nstored.as<int>();
+        a.ev_t = ev_t.as<R>();
+        a.ev_x = ev_x.as<R>();
+        a.ev_dx = ev_dx.as<R>();
+        a.ev_aux = ev_aux.as<R>();
+        a.n_events = nevents.as<int>();
+        a.ev_rows = ev_rows;
         a.status = status.as<int>();
         a.stats = collect_stats ? stats.as<unsigned long long>() : nullptr;
         a.work_next = work.as<unsigned int>();
@@ -733,6 +819,7 @@ struct clode_sim {
             fail(CLODE_ERR_STATE, "not a feature simulator");
         if (reinit >= 0)
             observer_initialized = reinit == 0;
+        want_store = false;
         ensure_built();
         resize_features();
         int fused = 0;
@@ -758,18 +845,63 @@ struct clode_sim {
         log_msg(CLODE_LOG_DEBUG, "run features");
     }
 
+    // Features with storage: the feature pass of features() that also
+    // stores the trajectory rows (as trajectory(): row 0 and every nout-th
+    // step, rows up to max_store) and the state at each of the first
+    // event_rows observer events of every member.  F, xf, dt, tf and the RNG
+    // state come out as from features(); the program is the features
+    // program compiled with CLODE_FEATURE_STORE.
+    void features_store(int reinit, unsigned int event_rows)
+    {
+        require_problem();
+        if (kind != CLODE_SIM_FEATURES)
+            fail(CLODE_ERR_STATE, "not a feature simulator");
+        if (sp.nout == 0)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "nout must be at least 1");
+        if (reinit >= 0)
+            observer_initialized = reinit == 0;
+        want_store = true;
+        ensure_built();
+        resize_features();
+        resize_trajectory();
+        resize_events(event_rows);
+        int fused = 0;
+        double init_ms = 0.0;
+        unsigned long long init_stats[CLODE_STAT_COUNT] = {0};
+        if (!observer_initialized) {
+            if (fuse_init) {
+                fused = 1;
+            } else {
+                initialize_observer();
+                init_ms = last_ms;
+                memcpy(init_stats, last_stats, sizeof init_stats);
+            }
+        }
+        begin_run();
+        launch(k_features, kp_features, fused);
+        end_run("features with storage");
+        last_ms += init_ms;
+        for (int k = 0; k < CLODE_STAT_COUNT; ++k)
+            last_stats[k] += init_stats[k];
+        observer_initialized = true;
+        events_valid = true;
+        log_msg(CLODE_LOG_DEBUG, "run features with storage");
+    }
+
     // CLODEtrajectory::resizeTrajectoryVariables (CLODEtrajectory.cpp:45-94)
     void resize_trajectory()
     {
         long long rows = (long long)sp.max_store + 1;  // the kernel may write row max_store
-        if (rows == traj_rows && nPts == traj_pts)
+        const int nv = store_nv(), na = store_na();
+        const long long width = 1 + 2 * nv + na;
+        if (rows == traj_rows && nPts == traj_pts && width == traj_width)
             return;
         size_t rs = real_size();
-        double need = (double)rows * nPts * (1 + 2 * nVar + nAux) * rs;
+        double need = (double)rows * nPts * width * rs;
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
         if (need > (double)free_b) {
-            long long max_rows = (long long)(free_b / ((double)nPts * (1 + 2 * nVar + nAux) * rs));
+            long long max_rows = (long long)(free_b / ((double)nPts * width * rs));
             log_msg(CLODE_LOG_ERR,
                     "Storage requested exceeds device memory. Try reducing storage to <%lld time points, or reducing nPts.",
                     max_rows);
@@ -777,21 +909,49 @@ struct clode_sim {
                  need / 1e9, free_b / 1e9);
         }
         t.reserve(std::max<size_t>(1, rows * nPts) * rs);
-        x.reserve(std::max<size_t>(1, rows * nPts * nVar) * rs);
-        dx.reserve(std::max<size_t>(1, rows * nPts * nVar) * rs);
-        aux.reserve(std::max<size_t>(1, rows * nPts * std::max(nAux, 1)) * rs);
+        x.reserve(std::max<size_t>(1, rows * nPts * nv) * rs);
+        dx.reserve(std::max<size_t>(1, rows * nPts * nv) * rs);
+        aux.reserve(std::max<size_t>(1, rows * nPts * std::max(na, 1)) * rs);
         nstored.reserve(std::max<size_t>(1, nPts) * sizeof(int));
         // rows a run does not reach read as zero after a resize, as in a
         // freshly created buffer, not as whatever the memory held before
         ensure_stream();
         check_cuda(cudaMemsetAsync(t.p, 0, (size_t)rows * nPts * rs, stream), "trajectory clear");
-        check_cuda(cudaMemsetAsync(x.p, 0, (size_t)rows * nPts * nVar * rs, stream), "trajectory clear");
-        check_cuda(cudaMemsetAsync(dx.p, 0, (size_t)rows * nPts * nVar * rs, stream), "trajectory clear");
-        if (nAux > 0)
-            check_cuda(cudaMemsetAsync(aux.p, 0, (size_t)rows * nPts * nAux * rs, stream), "trajectory clear");
+        check_cuda(cudaMemsetAsync(x.p, 0, (size_t)rows * nPts * nv * rs, stream), "trajectory clear");
+        check_cuda(cudaMemsetAsync(dx.p, 0, (size_t)rows * nPts * nv * rs, stream), "trajectory clear");
+        if (na > 0)
+            check_cuda(cudaMemsetAsync(aux.p, 0, (size_t)rows * nPts * na * rs, stream), "trajectory clear");
         check_cuda(cudaMemsetAsync(nstored.p, 0, (size_t)nPts * sizeof(int), stream), "trajectory clear");
         traj_rows = rows;
         traj_pts = nPts;
+        traj_width = width;
+    }
+
+    // event store of features with storage: ev_rows rows of (t, x, dx, aux)
+    void resize_events(unsigned int rows)
+    {
+        const int nv = store_nv(), na = store_na();
+        const long long width = 1 + 2 * nv + na;
+        ensure_stream();
+        if ((long long)rows != ev_rows_alloc || nPts != ev_pts || width != ev_width) {
+            size_t rs = real_size();
+            ev_t.reserve(std::max<size_t>(1, (size_t)rows * nPts) * rs);
+            ev_x.reserve(std::max<size_t>(1, (size_t)rows * nPts * nv) * rs);
+            ev_dx.reserve(std::max<size_t>(1, (size_t)rows * nPts * nv) * rs);
+            ev_aux.reserve(std::max<size_t>(1, (size_t)rows * nPts * std::max(na, 1)) * rs);
+            nevents.reserve(std::max<size_t>(1, nPts) * sizeof(int));
+            ev_rows_alloc = rows;
+            ev_pts = nPts;
+            ev_width = width;
+        }
+        // rows a member does not reach read as zero
+        size_t rs = real_size();
+        check_cuda(cudaMemsetAsync(ev_t.p, 0, (size_t)rows * nPts * rs, stream), "event store clear");
+        check_cuda(cudaMemsetAsync(ev_x.p, 0, (size_t)rows * nPts * nv * rs, stream), "event store clear");
+        check_cuda(cudaMemsetAsync(ev_dx.p, 0, (size_t)rows * nPts * nv * rs, stream), "event store clear");
+        if (na > 0)
+            check_cuda(cudaMemsetAsync(ev_aux.p, 0, (size_t)rows * nPts * na * rs, stream), "event store clear");
+        ev_rows = rows;
     }
 
     void trajectory()
@@ -1089,8 +1249,12 @@ struct clode_sim {
         case CLODE_ARRAY_F: return F_elements > 0 ? (size_t)F_elements : 0;
         case CLODE_ARRAY_T: return traj_rows > 0 ? (size_t)sp.max_store * nPts : 0;
         case CLODE_ARRAY_X:
-        case CLODE_ARRAY_DX: return traj_rows > 0 ? (size_t)sp.max_store * nPts * nVar : 0;
-        case CLODE_ARRAY_AUX: return traj_rows > 0 ? (nAux > 0 ? (size_t)sp.max_store * nPts * nAux : 1) : 0;
+        case CLODE_ARRAY_DX: return traj_rows > 0 ? (size_t)sp.max_store * nPts * store_nv() : 0;
+        case CLODE_ARRAY_AUX: return traj_rows > 0 ? (store_na() > 0 ? (size_t)sp.max_store * nPts * store_na() : 1) : 0;
+        case CLODE_ARRAY_EVENT_T: return events_valid ? (size_t)ev_rows * nPts : 0;
+        case CLODE_ARRAY_EVENT_X:
+        case CLODE_ARRAY_EVENT_DX: return events_valid ? (size_t)ev_rows * nPts * store_nv() : 0;
+        case CLODE_ARRAY_EVENT_AUX: return events_valid ? (size_t)ev_rows * nPts * store_na() : 0;
         }
         fail(CLODE_ERR_INVALID_ARGUMENT, "unknown array id %d", which);
     }
@@ -1122,14 +1286,67 @@ struct clode_sim {
         case CLODE_ARRAY_X: src = &x; break;
         case CLODE_ARRAY_DX: src = &dx; break;
         case CLODE_ARRAY_AUX:
-            if (nAux == 0) {
+            if (store_na() == 0) {
                 out[0] = 0.0;
                 return;
             }
             src = &aux;
             break;
+        case CLODE_ARRAY_EVENT_T: src = &ev_t; break;
+        case CLODE_ARRAY_EVENT_X: src = &ev_x; break;
+        case CLODE_ARRAY_EVENT_DX: src = &ev_dx; break;
+        case CLODE_ARRAY_EVENT_AUX: src = &ev_aux; break;
         }
         download(*src, out, n);
+    }
+
+    // Rows [0, rows) of members [first, first + count) of the last
+    // trajectory, regrouped member-major on the device (one transpose per
+    // stored array, see launch_regroup_by_member_*) and copied out in chunks
+    // of at most 256 MB of staging.  Null outputs are skipped.
+    void get_by_member(long long first, long long count, long long rows, double *t_out, double *x_out,
+                       double *dx_out, double *aux_out, int *nstored_out)
+    {
+        if (traj_rows <= 0)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "no trajectory has been run");
+        if (first < 0 || count < 0 || first + count > nPts)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "members [%lld, %lld) are outside [0, %lld)", first, first + count,
+                 nPts);
+        if (rows < 0 || rows > (long long)sp.max_store)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "rows = %lld is outside [0, max_store = %u]", rows, sp.max_store);
+        if (!count)
+            return;
+        ensure_stream();
+        if (nstored_out)
+            check_cuda(cudaMemcpyAsync(nstored_out, nstored.as<int>() + first, (size_t)count * sizeof(int),
+                                       cudaMemcpyDeviceToHost, stream),
+                       "D2H copy");
+        struct Part {
+            const DevBuf *src;
+            double *out;
+            size_t width;
+        } parts[4] = {{&t, t_out, 1}, {&x, x_out, (size_t)store_nv()}, {&dx, dx_out, (size_t)store_nv()},
+                      {&aux, aux_out, (size_t)store_na()}};
+        const size_t stage_max = (size_t)256 << 20;
+        for (const Part &p : parts) {
+            if (!p.out || p.width == 0 || rows == 0)
+                continue;
+            const size_t nc = (size_t)rows * p.width, per_member = nc * sizeof(double);
+            const size_t chunk = std::max<size_t>(1, std::min<size_t>((size_t)count, stage_max / per_member));
+            stage.reserve(chunk * per_member);
+            for (size_t m = 0; m < (size_t)count; m += chunk) {
+                const size_t nm = std::min<size_t>(chunk, (size_t)count - m);
+                if (single)
+                    launch_regroup_by_member_f32(p.src->as<float>(), (size_t)nPts, (size_t)first + m, nm, nc,
+                                                 stage.as<double>(), stream);
+                else
+                    launch_regroup_by_member_f64(p.src->as<double>(), (size_t)nPts, (size_t)first + m, nm, nc,
+                                                 stage.as<double>(), stream);
+                check_cuda(cudaMemcpyAsync(p.out + m * nc, stage.p, nm * per_member, cudaMemcpyDeviceToHost, stream),
+                           "D2H copy");
+            }
+        }
+        check_cuda(cudaStreamSynchronize(stream), "D2H copy");
     }
 
     std::string status_report() const
@@ -1434,6 +1651,9 @@ int clode_sim_get_sizes(clode_sim *sim, clode_sizes *out)
         out->t_elements = (long long)sim->array_len(CLODE_ARRAY_T);
         out->x_elements = (long long)sim->array_len(CLODE_ARRAY_X);
         out->aux_elements = (long long)sim->array_len(CLODE_ARRAY_AUX);
+        out->n_store_var = sim->store_nv();
+        out->n_store_aux = sim->store_na();
+        out->event_rows = sim->events_valid ? sim->ev_rows : 0;
     });
 }
 
@@ -1463,6 +1683,38 @@ int clode_sim_get_n_stored(clode_sim *sim, int *out, size_t capacity, size_t *n)
             fail(CLODE_ERR_INVALID_ARGUMENT, "output capacity %zu is smaller than nPts (%zu)", capacity, len);
         sim->ensure_stream();
         check_cuda(cudaMemcpy(out, sim->nstored.p, len * sizeof(int), cudaMemcpyDeviceToHost), "D2H copy");
+    });
+}
+
+int clode_sim_get_trajectory_by_member(clode_sim *sim, long long first, long long count, long long rows,
+                                       double *t_out, double *x_out, double *dx_out, double *aux_out,
+                                       int *n_stored_out)
+{
+    SIM_GUARD({ sim->get_by_member(first, count, rows, t_out, x_out, dx_out, aux_out, n_stored_out); });
+}
+
+int clode_sim_features_store(clode_sim *sim, int initialize_observer, unsigned int event_rows)
+{
+    SIM_GUARD(sim->features_store(initialize_observer, event_rows));
+}
+
+int clode_sim_set_store_variables(clode_sim *sim, const int *var_ix, int n_var_ix, const int *aux_ix, int n_aux_ix)
+{
+    SIM_GUARD(sim->set_store_variables(var_ix, n_var_ix, aux_ix, n_aux_ix));
+}
+
+int clode_sim_get_n_events(clode_sim *sim, int *out, size_t capacity, size_t *n)
+{
+    SIM_GUARD({
+        size_t len = sim->events_valid ? (size_t)sim->nPts : 0;
+        if (n)
+            *n = len;
+        if (!out || !len)
+            return;
+        if (capacity < len)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "output capacity %zu is smaller than nPts (%zu)", capacity, len);
+        sim->ensure_stream();
+        check_cuda(cudaMemcpy(out, sim->nevents.p, len * sizeof(int), cudaMemcpyDeviceToHost), "D2H copy");
     });
 }
 

@@ -62,7 +62,14 @@ enum clode_array {
     CLODE_ARRAY_T = 7,      /* CLODEtrajectory::getT       clode/cpp/CLODEtrajectory.cpp:132 */
     CLODE_ARRAY_X = 8,      /* CLODEtrajectory::getX       clode/cpp/CLODEtrajectory.cpp:149 */
     CLODE_ARRAY_DX = 9,     /* CLODEtrajectory::getDx      clode/cpp/CLODEtrajectory.cpp:166 */
-    CLODE_ARRAY_AUX = 10    /* CLODEtrajectory::getAux     clode/cpp/CLODEtrajectory.cpp:183 */
+    CLODE_ARRAY_AUX = 10,   /* CLODEtrajectory::getAux     clode/cpp/CLODEtrajectory.cpp:183 */
+    /* event states of clode_sim_features_store(), [k*nPts*w + j*nPts + i]
+     * (the t_event/x_event/dx_event/aux_event buffers of the reference's
+     * unused clode/cpp/odedriver.cl:27-30) */
+    CLODE_ARRAY_EVENT_T = 11,
+    CLODE_ARRAY_EVENT_X = 12,
+    CLODE_ARRAY_EVENT_DX = 13,
+    CLODE_ARRAY_EVENT_AUX = 14
 };
 
 /* strings readable with clode_sim_get_string() */
@@ -211,6 +218,8 @@ typedef struct clode_sizes {
     long long n_pts, n_var, n_par, n_aux, n_wiener, n_features;
     long long max_store;         /* rows of the trajectory arrays */
     long long t_elements, x_elements, aux_elements;
+    long long n_store_var, n_store_aux;  /* stored columns of x/dx and of aux per row */
+    long long event_rows;                /* rows of the event arrays (0 before clode_sim_features_store) */
 } clode_sizes;
 int clode_sim_get_sizes(clode_sim *sim, clode_sizes *out);
 /* copy an array to host doubles; *n receives its length. With out == NULL only *n is set. */
@@ -227,6 +236,38 @@ int clode_sim_set_tspan_per_member(clode_sim *sim, const double *tspan, size_t n
  * larger ensemble continue exactly the streams the full ensemble would use. */
 int clode_sim_get_rng_state(clode_sim *sim, unsigned long long *out, size_t capacity, size_t *n);
 int clode_sim_set_rng_state(clode_sim *sim, const unsigned long long *state, size_t n);
+/* The last trajectory regrouped by member, as the per-member arrays that
+ * clODE's TrajectorySimulator.get_trajectory slices out of getT/getX/getDx/
+ * getAux on the host (clode/trajectory.py:216-264): for members i in
+ * [first, first + count) and rows r < rows (rows <= max_store),
+ *   t_out[(i - first) * rows + r]
+ *   x_out[((i - first) * rows + r) * nVar + j], dx_out likewise,
+ *   aux_out[((i - first) * rows + r) * nAux + k],
+ *   n_stored_out[i - first] (CLODEtrajectory::getNstored).
+ * The regrouping runs on the device; any output may be NULL to skip it. */
+int clode_sim_get_trajectory_by_member(clode_sim *sim, long long first, long long count, long long rows,
+                                       double *t_out, double *x_out, double *dx_out, double *aux_out,
+                                       int *n_stored_out);
+/* Features with storage, one pass (the design of the reference's unused
+ * unified driver clode/cpp/odedriver.cl:10-162, repaired): the features run
+ * of clode_sim_features() (same F, xf, dt, tf, RNG state) that also stores
+ * the trajectory rows of that pass exactly as clode_sim_trajectory() stores
+ * them (row 0 and every nout-th step, at most max_store + 1 rows; a full
+ * buffer ends the storing, not the integration), readable with the
+ * CLODE_ARRAY_T..AUX getters, clode_sim_get_n_stored() and
+ * clode_sim_get_trajectory_by_member(); and the state (t, x, dx, aux) at
+ * each of the first event_rows observer events of every member
+ * (CLODE_ARRAY_EVENT_*, clode_sim_get_n_events()).  initialize_observer as
+ * in clode_sim_features(). */
+int clode_sim_features_store(clode_sim *sim, int initialize_observer, unsigned int event_rows);
+/* Events each member met in the feature pass of the last clode_sim_features_store() */
+int clode_sim_get_n_events(clode_sim *sim, int *out, size_t capacity, size_t *n);
+/* Stored columns of trajectories and event states: the variables var_ix[0..n_var_ix)
+ * and auxiliary variables aux_ix[0..n_aux_ix), in that order (the option
+ * clode/cpp/trajectory.cl:3 leaves as a TODO).  A negative count keeps all of
+ * them; both negative restore the reference layout.  Takes effect at the next
+ * run (the program is rebuilt with the lists compiled in). */
+int clode_sim_set_store_variables(clode_sim *sim, const int *var_ix, int n_var_ix, const int *aux_ix, int n_aux_ix);
 /* Per-member status bits of the last run (CLODE_MEMBER_*). */
 int clode_sim_get_status(clode_sim *sim, int *out, size_t capacity, size_t *n);
 /* Launch-wide counters of the last run (CLODE_STAT_*; out has CLODE_STAT_COUNT slots). */
