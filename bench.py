@@ -328,6 +328,51 @@ def bench_trajectory_frontend(W, pi, pars, tuned_options: dict, args) -> dict:
             "speedup": min(ref) / min(ours)}
 
 
+def bench_feature_store(args, tuned_options: dict) -> dict:
+    """Features and stored trajectories in one pass (features_store) against
+    the two runs it replaces (features, then trajectory): the lactotroph
+    model on a 256 x 256 grid of (gcal, gbk), tspan [0, 3000] ms, DP45 rtol
+    1e-6 FP32, nhood2; a row every 50 steps and the first 16 event states
+    per member.  Device time of each call (observer initialisation
+    included), best of 3."""
+    from clode_gb300 import clode_cpp_wrapper as W, rhs_path
+
+    grid = 256
+    x0, pars, _ = make_workload(grid, args.seed, args.tmin, args.tmax)
+    pi = W.ProblemInfo(rhs_path("lactotroph.cl"), ["v", "n", "f", "c"], ["gcal", "gsk", "gbk"], ["ica"], 0)
+    sp = W.SolverParams(dt=SOLVER["dt"], dtmax=SOLVER["dtmax"], abstol=1e-6, reltol=1e-6,
+                        max_steps=SOLVER["max_steps"], max_store=1000, nout=50)
+    op = W.ObserverParams(**OBSERVER)
+
+    def setup(sim, traj=False):
+        for k, v in tuned_options.items():
+            if not (traj and k == "fuse_init"):
+                sim.set_option(k, v)
+        sim.set_solver_params(sp)
+        sim.set_problem_data(x0.flatten(order="F"), pars.flatten(order="F"))
+        sim.set_tspan([0.0, 3000.0])
+        return sim
+
+    store = setup(W.FeatureSimulatorBase(pi, "dopri5", "nhood2", op, True, W.OpenCLResource(), ""))
+    plain = setup(W.FeatureSimulatorBase(pi, "dopri5", "nhood2", op, True, W.OpenCLResource(), ""))
+    traj = setup(W.TrajectorySimulatorBase(pi, "dopri5", True, W.OpenCLResource(), ""), traj=True)
+    t_store, t_sep = [], []
+    for _ in range(3):  # each run continues from the step sizes the previous one ended with, in all three
+        store.features_store(True, event_rows=16)
+        t_store.append(store.last_kernel_ms())
+        plain.features(True)
+        ms = plain.last_kernel_ms()
+        traj.trajectory()
+        t_sep.append(ms + traj.last_kernel_ms())
+    same = bool(np.array_equal(store.get_n_stored(), traj.get_n_stored()))
+    return {"workload": f"lactotroph nhood2, {grid}x{grid} (gcal, gbk) grid, tspan [0, 3000] ms, DP45 rtol 1e-6 "
+                        "FP32, a row every 50 steps, 16 event states per member",
+            "members": grid * grid, "rows_max": int(store.get_n_stored().max()) + 1,
+            "events_max": int(store.get_n_events().max()),
+            "one_pass_ms": min(t_store), "two_runs_ms": min(t_sep), "speedup": min(t_sep) / min(t_store),
+            "rows_identical_to_trajectory_run": same}
+
+
 def bench_reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -389,6 +434,8 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-trajectory", action="store_true")
     ap.add_argument("--trajectory-steps", type=int, default=100000)
+    ap.add_argument("--feature-store", type=int, default=1,
+                    help="1: also time features with storage against separate features and trajectory runs")
     ap.add_argument("--trajectory-frontend", type=int, default=1,
                     help="1: also time per-member trajectory outputs against clODE's per-member loop")
     ap.add_argument("--no-cpu", action="store_true")
@@ -583,6 +630,11 @@ def main():
             line["trajectory"] = bench_trajectory(args, opts)
         except Exception as e:
             line["trajectory"] = {"error": f"{type(e).__name__}: {e}"}
+    if rank == 0 and args.feature_store:
+        try:
+            line["feature_store"] = bench_feature_store(args, opts)
+        except Exception as e:
+            line["feature_store"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

@@ -1754,6 +1754,13 @@ int clode_sim_set_rng_state(clode_sim *sim, const unsigned long long *state, siz
         if (sim->nPts <= 0 || n != 2 * (size_t)sim->nPts)
             fail(CLODE_ERR_INVALID_ARGUMENT, "RNG state needs 2*nPts=%lld words, received %zu", 2 * sim->nPts, n);
         need(state, "state");
+        // (0, 0) is xoroshiro128+'s fixed point: the polar method would draw
+        // rejected candidates from it forever (clode/cpp/clODE_random.cl:88-114)
+        const long long np = sim->nPts;
+        for (long long i = 0; i < np; ++i)
+            if (state[i] == 0 && state[np + i] == 0)
+                fail(CLODE_ERR_INVALID_ARGUMENT,
+                     "member %lld: the all-zero RNG state is the generator's fixed point and never yields a normal", i);
         sim->ensure_stream();
         check_cuda(cudaMemcpy(sim->rng.p, state, n * sizeof(unsigned long long), cudaMemcpyHostToDevice), "H2D copy");
     });

@@ -233,7 +233,10 @@ int clode_sim_get_string(clode_sim *sim, int which, char *buf, size_t capacity, 
 int clode_sim_set_tspan_per_member(clode_sim *sim, const double *tspan, size_t n);
 /* Raw per-member RNG state: 2*nPts u64 words laid out [j*nPts + i] as the
  * kernels read it (clode/cpp/transient.cl:37-39).  Setting it lets a shard of a
- * larger ensemble continue exactly the streams the full ensemble would use. */
+ * larger ensemble continue exactly the streams the full ensemble would use.
+ * A member whose two words are both zero (the generator's fixed point, from
+ * which no normal deviate can ever be accepted) is refused with
+ * CLODE_ERR_INVALID_ARGUMENT and nothing is changed. */
 int clode_sim_get_rng_state(clode_sim *sim, unsigned long long *out, size_t capacity, size_t *n);
 int clode_sim_set_rng_state(clode_sim *sim, const unsigned long long *state, size_t n);
 /* The last trajectory regrouped by member, as the per-member arrays that

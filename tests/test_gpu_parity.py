@@ -240,17 +240,21 @@ def test_split_attempts_bitwise(stepper, kind):
         assert eng["stats"][0]["rejected"] == ref["stats"][0]["rejected"]
 
 
-def test_persistent_stochastic_bitwise_rng_state():
-    # seuler in FP64 on the OU process: the normal deviates use log, so the
-    # states are compared with a tolerance, but the RNG words must be equal
+@pytest.mark.parametrize("single", [False, True], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("schedule", [0, 1], ids=["grid", "persistent"])
+def test_stochastic_bitwise_rng_state(single, schedule):
+    # seuler on the OU process, two launches in a row: the RNG words the
+    # engine stores after each launch must be the oracle's, whatever lanes
+    # of a warp drew ahead of need (the look-ahead is undone before the
+    # store), and in FP32 whichever conversion of the u64 words ran.  The
+    # deviates use log, so the states are compared with a tolerance.
     n = 3000
     rng = np.random.default_rng(5)
     pars = np.stack([rng.uniform(0.1, 2, n), np.zeros(n), rng.uniform(0.1, 1, n)], axis=1)
     sc = Scenario("ornstein_uhlenbeck.cl", 1, 3, np.zeros((n, 1)), pars, n_wiener=1, stepper="seuler",
-                  single=False, sp=dict(dt=1e-3, max_steps=3000), seed=99,
-                  steps=[("transient", (0.0, 2.0))])
-    eng = run_engine(sc, options=PERSISTENT)
-    ora_sim_state = None
+                  single=single, sp=dict(dt=1e-3, max_steps=3000), seed=99,
+                  steps=[("transient", (0.0, 2.0)), ("shift_x0",), ("transient", (0.0, 1.5))])
+    eng = run_engine(sc, options={"schedule": schedule})
     from oracle.runner import OracleSimulator
     s = OracleSimulator(sc.oracle_config())
     s.set_solver_params(dt=1e-3, dtmax=0.5, abstol=1e-6, reltol=1e-3, max_steps=3000, max_store=1, nout=1)
@@ -258,10 +262,37 @@ def test_persistent_stochastic_bitwise_rng_state():
     s.seed_rng(99)
     s.set_tspan((0.0, 2.0))
     s.transient()
-    ora_sim_state = s.rng.copy()
-    np.testing.assert_array_equal(eng["sim"].get_rng_state(), ora_sim_state)
+    s.shift_x0()
+    s.set_tspan((0.0, 1.5))
+    s.transient()
+    np.testing.assert_array_equal(eng["sim"].get_rng_state(), s.rng)
     # tolerance: log() of the polar method may differ by an ulp from the host libm
-    np.testing.assert_allclose(eng["xf"], s.get_xf(), rtol=1e-9, atol=1e-12)
+    if single:
+        np.testing.assert_allclose(eng["xf"], s.get_xf(), rtol=1e-3, atol=2e-5)
+    else:
+        np.testing.assert_allclose(eng["xf"], s.get_xf(), rtol=1e-9, atol=1e-12)
+
+
+def test_all_zero_rng_state_is_rejected():
+    # (0, 0) is xoroshiro128+'s fixed point: the polar method would reject
+    # every candidate drawn from it, so such a state is refused on the host
+    # and the stored state stays as it was
+    from clode_gb300 import clode_cpp_wrapper as W, rhs_path
+    n = 16
+    pi = W.ProblemInfo(rhs_path("ornstein_uhlenbeck.cl"), ["x"], ["theta", "mu", "sigma"], [], 1)
+    sim = W.SimulatorBase(pi, "seuler", True, W.OpenCLResource(), "")
+    sim.set_problem_data(np.zeros(n), np.tile([1.0, 0.0, 0.5], (n, 1)).flatten(order="F"))
+    sim.seed_rng(3)
+    before = sim.get_rng_state()
+    st = before.copy()
+    st[5] = st[n + 5] = 0
+    with pytest.raises(W.ClodeValueError, match="fixed point"):
+        sim.set_rng_state(st)
+    assert np.array_equal(sim.get_rng_state(), before)
+    st = before.copy()
+    st[5] = 0  # one zero word is a valid state
+    sim.set_rng_state(st)
+    assert np.array_equal(sim.get_rng_state(), st)
 
 
 def test_time_budget_marks_unprocessed_members():
