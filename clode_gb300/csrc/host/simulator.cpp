@@ -512,6 +512,7 @@ struct clode_sim {
     {
         if (n == 0)
             return;
+        HostPin pin(const_cast<double *>(src), n * sizeof(double));
         if (single) {
             stage.reserve(n * sizeof(double));
             check_cuda(cudaMemcpyAsync(stage.p, src, n * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D copy");
@@ -522,10 +523,35 @@ struct clode_sim {
         check_cuda(cudaStreamSynchronize(stream), "H2D copy");
     }
 
+    // Page-locks a large caller-owned host range while it receives a copy,
+    // so the device-to-host transfer runs at the link's rate instead of
+    // through the driver's pageable staging.  A range that cannot be
+    // registered (or already is) is copied as it is.
+    struct HostPin {
+        void *p = nullptr;
+        HostPin(void *ptr, size_t bytes)
+        {
+            if (ptr && bytes >= ((size_t)32 << 20)) {
+                if (cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess)
+                    p = ptr;
+                else
+                    (void)cudaGetLastError();
+            }
+        }
+        ~HostPin()
+        {
+            if (p)
+                cudaHostUnregister(p);
+        }
+        HostPin(const HostPin &) = delete;
+        HostPin &operator=(const HostPin &) = delete;
+    };
+
     void download(const DevBuf &src, double *dst, size_t n)
     {
         if (n == 0)
             return;
+        HostPin pin(dst, n * sizeof(double));
         if (single) {
             stage.reserve(n * sizeof(double));
             launch_f32_to_f64(src.as<float>(), stage.as<double>(), n, stream);
@@ -1334,6 +1360,7 @@ struct clode_sim {
             const size_t nc = (size_t)rows * p.width, per_member = nc * sizeof(double);
             const size_t chunk = std::max<size_t>(1, std::min<size_t>((size_t)count, stage_max / per_member));
             stage.reserve(chunk * per_member);
+            HostPin pin(p.out, (size_t)count * per_member);
             for (size_t m = 0; m < (size_t)count; m += chunk) {
                 const size_t nm = std::min<size_t>(chunk, (size_t)count - m);
                 if (single)
@@ -1345,6 +1372,7 @@ struct clode_sim {
                 check_cuda(cudaMemcpyAsync(p.out + m * nc, stage.p, nm * per_member, cudaMemcpyDeviceToHost, stream),
                            "D2H copy");
             }
+            check_cuda(cudaStreamSynchronize(stream), "D2H copy");  // before the range is unpinned
         }
         check_cuda(cudaStreamSynchronize(stream), "D2H copy");
     }
