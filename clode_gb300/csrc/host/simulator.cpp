@@ -382,6 +382,14 @@ struct clode_sim {
         }
     }
 
+    // Rows the trajectory getters return: max_store, as CLODEtrajectory's
+    // getters copy (CLODEtrajectory.cpp:132-200), but never more than the
+    // buffers of the last run hold (max_store may have grown since).
+    size_t stored_rows() const
+    {
+        return traj_rows > 0 ? std::min<size_t>(sp.max_store, (size_t)traj_rows - 1) : 0;
+    }
+
     // ------------------------------------------------------------ build --
     static std::string join_ix(const std::vector<int> &v)
     {
@@ -599,6 +607,8 @@ struct clode_sim {
         fill_real(dt, sp.dt, n);
         F_elements = -1;
         traj_rows = -1;
+        events_valid = false;
+        ev_rows_alloc = -1;  // event buffers are re-made for the new size or precision
         observer_initialized = false;
         if (tspan_per_member && (long long)tspan_pm.size() != 2 * n) {
             tspan_per_member = false;
@@ -1273,10 +1283,10 @@ struct clode_sim {
         case CLODE_ARRAY_PARS: return pars_host.size();
         case CLODE_ARRAY_TSPAN: return tspan_per_member ? tspan_pm.size() : 2;
         case CLODE_ARRAY_F: return F_elements > 0 ? (size_t)F_elements : 0;
-        case CLODE_ARRAY_T: return traj_rows > 0 ? (size_t)sp.max_store * nPts : 0;
+        case CLODE_ARRAY_T: return traj_rows > 0 ? stored_rows() * nPts : 0;
         case CLODE_ARRAY_X:
-        case CLODE_ARRAY_DX: return traj_rows > 0 ? (size_t)sp.max_store * nPts * store_nv() : 0;
-        case CLODE_ARRAY_AUX: return traj_rows > 0 ? (store_na() > 0 ? (size_t)sp.max_store * nPts * store_na() : 1) : 0;
+        case CLODE_ARRAY_DX: return traj_rows > 0 ? stored_rows() * nPts * store_nv() : 0;
+        case CLODE_ARRAY_AUX: return traj_rows > 0 ? (store_na() > 0 ? stored_rows() * nPts * store_na() : 1) : 0;
         case CLODE_ARRAY_EVENT_T: return events_valid ? (size_t)ev_rows * nPts : 0;
         case CLODE_ARRAY_EVENT_X:
         case CLODE_ARRAY_EVENT_DX: return events_valid ? (size_t)ev_rows * nPts * store_nv() : 0;
@@ -1338,8 +1348,9 @@ struct clode_sim {
         if (first < 0 || count < 0 || first + count > nPts)
             fail(CLODE_ERR_INVALID_ARGUMENT, "members [%lld, %lld) are outside [0, %lld)", first, first + count,
                  nPts);
-        if (rows < 0 || rows > (long long)sp.max_store)
-            fail(CLODE_ERR_INVALID_ARGUMENT, "rows = %lld is outside [0, max_store = %u]", rows, sp.max_store);
+        if (rows < 0 || rows > (long long)stored_rows())
+            fail(CLODE_ERR_INVALID_ARGUMENT, "rows = %lld is outside [0, %zu] (max_store of the stored run)", rows,
+                 stored_rows());
         if (!count)
             return;
         ensure_stream();

@@ -94,3 +94,19 @@ def test_regroup_rejects_bad_ranges():
         sim.get_trajectory_by_member(rows=51)
     with pytest.raises(Exception):
         sim.get_trajectory_by_member(first=-1, count=3)
+
+
+def test_getters_stay_within_the_stored_run():
+    # max_store raised after the run: the getters return the rows the run's
+    # buffers hold, never more, until the next run resizes them
+    sim, _ = _lactotroph(True, n=40, max_store=50)
+    t_before = sim.get_t()
+    assert t_before.size == 50 * 40
+    sim.set_solver_params(W.SolverParams(dt=0.1, dtmax=10.0, abstol=1e-6, reltol=1e-6, max_steps=100000,
+                                         max_store=500, nout=3))
+    assert np.array_equal(sim.get_t(), t_before)
+    assert sim.get_x().size == 50 * 4 * 40
+    with pytest.raises(Exception):
+        sim.get_trajectory_by_member(rows=51)
+    sim.trajectory()
+    assert sim.get_t().size == 500 * 40
