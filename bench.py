@@ -328,6 +328,105 @@ def bench_trajectory_frontend(W, pi, pars, tuned_options: dict, args) -> dict:
             "speedup": min(ref) / min(ours)}
 
 
+def bench_configs(args, tuned_options: dict) -> dict:
+    """The two other deterministic workloads of the scope, timed on the device
+    (CUDA events, observer initialisation included, best of 3):
+
+    * Van der Pol, 4,096 members, mu ~ U[0.1, 5], (x0, y0) ~ U[-2, 2]^2
+      (seeded), RK4 dt = 0.01 in FP64: transient [0, 200] (20,001 steps),
+      then localmax features on x over [200, 1000] (80,001 steps).  Bound:
+      the FP64 pipe (nominal 1.25 TFLOP/s on GB300).
+    * Lorenz, 1024 x 1024 grid of sigma = linspace(5, 15) x rho =
+      linspace(10, 60), beta = 8/3, x0 = (1, 1, 1) + N(0, 1e-6) (seeded),
+      DP45 rtol 1e-6 atol 1e-9 dt0 1e-3 dtmax 1 in FP32 over [0, 500],
+      thresh2 on z (up 0.3, down 0.2, at most 1e5 events).  Bound: the FP32
+      pipe.  An absolute tolerance of 1e-9 is below FP32 resolution for
+      some members (about one in 2.6e5): their step size falls to its floor
+      and they run until max_steps, one lane alone for seconds while the
+      rest of the map takes a fraction of that; max_steps is 1e6 here
+      (the median member takes about 2.3e4 steps per pass) and the members
+      that reach it are counted in the line.
+
+    Flops are counted as for the lactotroph map: per RHS evaluation the
+    model's + - * / (Van der Pol 5, Lorenz 9), per RK4 step 14 n + 3, per
+    DP45 attempt 62 n + 10, per observer step 5 n + 3 n_aux + 6, with steps,
+    attempts and evaluations counted on the device."""
+    from clode_gb300 import clode_cpp_wrapper as W, rhs_path
+
+    out = {}
+    # Van der Pol, RK4, FP64
+    rng = np.random.default_rng(args.seed)
+    n = 4096
+    mu = rng.uniform(0.1, 5.0, n)
+    x0 = rng.uniform(-2.0, 2.0, (n, 2))
+    pi = W.ProblemInfo(rhs_path("van_der_pol.cl"), ["x", "y"], ["mu"], [], 0)
+    sim = W.FeatureSimulatorBase(pi, "rk4", "localmax", W.ObserverParams(e_var_ix=0, f_var_ix=0,
+                                                                        max_event_count=10000000),
+                                 False, W.OpenCLResource(), "")
+    for k in ("schedule", "block_size", "fmad"):
+        if k in tuned_options:
+            sim.set_option(k, tuned_options[k])
+    sim.set_solver_params(W.SolverParams(dt=0.01, dtmax=0.01, max_steps=10000000))
+    times, stats = [], None
+    for _ in range(3):
+        sim.set_problem_data(x0.flatten(order="F"), mu)
+        sim.set_tspan([0.0, 200.0])
+        sim.transient()
+        ms, st = sim.last_kernel_ms(), sim.get_stats()
+        sim.shift_x0()
+        sim.set_tspan([200.0, 1000.0])
+        sim.features(True)
+        ms += sim.last_kernel_ms()
+        st2 = sim.get_stats()
+        times.append(ms)
+        stats = {k: st[k] + st2[k] for k in ("steps", "rhs_evals")}
+    flops = stats["rhs_evals"] * 5 + stats["steps"] * (14 * 2 + 3) + st2["steps"] * (5 * 2 + 6)
+    ms = min(times)
+    fp64_peak = 1.25
+    out["vdp_rk4_fp64"] = {
+        "members": n, "steps": stats["steps"], "rhs_evals": stats["rhs_evals"], "ms": ms,
+        "points_per_s": n / (ms / 1e3), "rhs_evals_per_s": stats["rhs_evals"] / (ms / 1e3),
+        "roofline": {"bound": "fp64", "achieved": flops / (ms / 1e3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": flops / (ms / 1e3) / 1e12 / fp64_peak,
+                     "peak_source": "nominal GB300 FP64 rate (MEASURED_PEAKS.json has no FP64 figure)"}}
+
+    # Lorenz, DP45, FP32, thresh2
+    g = 1024
+    sig, rho = np.meshgrid(np.linspace(5.0, 15.0, g), np.linspace(10.0, 60.0, g), indexing="xy")
+    n = g * g
+    x0 = np.ones((n, 3)) + rng.normal(0.0, 1e-3, (n, 3))
+    pars = np.stack([rho.ravel(), sig.ravel(), np.full(n, 8.0 / 3.0)], axis=1)
+    pi = W.ProblemInfo(rhs_path("lorenz.cl"), ["x", "y", "z"], ["rho", "sigma", "beta"], ["fx"], 0)
+    sim = W.FeatureSimulatorBase(pi, "dopri5", "thresh2",
+                                 W.ObserverParams(e_var_ix=2, f_var_ix=2, max_event_count=100000,
+                                                  x_up_threshold=0.3, x_down_threshold=0.2),
+                                 True, W.OpenCLResource(), "")
+    for k, v in tuned_options.items():
+        sim.set_option(k, v)
+    sim.set_solver_params(W.SolverParams(dt=1e-3, dtmax=1.0, abstol=1e-9, reltol=1e-6, max_steps=1000000))
+    times = []
+    for _ in range(3):
+        sim.set_problem_data(x0.flatten(order="F"), pars.flatten(order="F"))  # same size: dt continues
+        sim.set_tspan([0.0, 500.0])
+        sim.features(True)
+        times.append(sim.last_kernel_ms())
+    st = sim.get_stats()
+    attempts = st["steps"] + st["rejected"]
+    flops = st["rhs_evals"] * 9 + attempts * (62 * 3 + 10) + st["steps"] * (5 * 3 + 3 + 6)
+    ms = min(times)
+    peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    status = sim.get_status()
+    out["lorenz_dp45_fp32"] = {
+        "members": n, "steps": st["steps"], "rejected": st["rejected"], "rhs_evals": st["rhs_evals"], "ms": ms,
+        "max_steps": 1000000, "members_at_max_steps": int(((status & 4) != 0).sum()),
+        "members_hmin_fail": int(((status & 1) != 0).sum()),
+        "points_per_s": n / (ms / 1e3), "rhs_evals_per_s": st["rhs_evals"] / (ms / 1e3),
+        "roofline": {"bound": "fp32", "achieved": flops / (ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                     "frac": flops / (ms / 1e3) / 1e12 / peak,
+                     "peak_source": "nominal FP32 FMA rate 152 SMs x 128 lanes x 2 at 2070 MHz"}}
+    return out
+
+
 def bench_feature_store(args, tuned_options: dict) -> dict:
     """Features and stored trajectories in one pass (features_store) against
     the two runs it replaces (features, then trajectory): the lactotroph
@@ -434,6 +533,8 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-trajectory", action="store_true")
     ap.add_argument("--trajectory-steps", type=int, default=100000)
+    ap.add_argument("--configs", type=int, default=1,
+                    help="1: also time the Van der Pol (RK4 FP64) and Lorenz (DP45 FP32) workloads")
     ap.add_argument("--feature-store", type=int, default=1,
                     help="1: also time features with storage against separate features and trajectory runs")
     ap.add_argument("--trajectory-frontend", type=int, default=1,
@@ -630,6 +731,11 @@ def main():
             line["trajectory"] = bench_trajectory(args, opts)
         except Exception as e:
             line["trajectory"] = {"error": f"{type(e).__name__}: {e}"}
+    if rank == 0 and args.configs:
+        try:
+            line["configs"] = bench_configs(args, opts)
+        except Exception as e:
+            line["configs"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and args.feature_store:
         try:
             line["feature_store"] = bench_feature_store(args, opts)
