@@ -533,6 +533,8 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-trajectory", action="store_true")
     ap.add_argument("--trajectory-steps", type=int, default=100000)
+    ap.add_argument("--order-by-span", type=int, default=None,
+                    help="persistent lanes take the longest time spans first (engine default 1)")
     ap.add_argument("--configs", type=int, default=1,
                     help="1: also time the Van der Pol (RK4 FP64) and Lorenz (DP45 FP32) workloads")
     ap.add_argument("--feature-store", type=int, default=1,
@@ -569,7 +571,8 @@ def main():
     for key, val in (("prec_div", args.prec_div), ("ftz", args.ftz), ("fast_math", args.fast_math),
                      ("fast_exp", args.fast_exp), ("split_attempts", args.split_attempts),
                      ("fuse_init", args.fuse_init), ("step_block", args.step_block),
-                     ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm)):
+                     ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm),
+                     ("order_by_span", args.order_by_span)):
         if val is not None:
             sim.set_option(key, val)
     sim.build_cl()

@@ -65,7 +65,7 @@ def _write_device_headers() -> str:
 
 
 def _sources() -> list[str]:
-    return [os.path.join(HOST_DIR, fn) for fn in ("runtime.cpp", "simulator.cpp", "aot_kernels.cu", "noalloc.cu",
+    return [os.path.join(HOST_DIR, fn) for fn in ("runtime.cpp", "simulator.cpp", "aot_kernels.cu", "order.cu", "noalloc.cu",
                                                   "mlp.cu", "mlp_net.cpp")]
 
 

@@ -98,6 +98,9 @@ struct ArgsT {
     // persistent scheduling: next member to hand out, and a %globaltimer budget in ns (0 = none)
     unsigned int *work_next;
     unsigned long long time_budget_ns;
+    // persistent kernels: position k of the range runs member order[k]
+    // (null: member k), e.g. the longest time spans first
+    const int *order;
     SolverParamsT<R> sp;
     ObserverParamsT<R> op;
 };

@@ -146,8 +146,9 @@ __device__ __forceinline__ void flush_counters(const Args &a, const Counters &c)
 #endif
 
 // Persistent schedule: hand out the next members of [i_begin, i_end) (every
-// i_stride-th one when i_stride > 1, as the autotuner samples) to the lanes of
-// this warp that ask for one, with a single atomic per warp.  Every lane of
+// i_stride-th one when i_stride > 1, as the autotuner samples; through the
+// permutation `order` when the host gives one) to the lanes of this warp that
+// ask for one, with a single atomic per warp.  Every lane of
 // the warp must call it (full-mask vote); lanes with want == false get -1.
 // Returns -1 as well once the range is exhausted.
 __device__ __forceinline__ int fetch_member(const Args &a, bool want)
@@ -165,7 +166,9 @@ __device__ __forceinline__ int fetch_member(const Args &a, bool want)
         return -1;
     const long long stride = a.i_stride > 1 ? a.i_stride : 1;
     long long k = (long long)a.i_begin + ((long long)base + __popc(mask & ((1u << lane) - 1u))) * stride;
-    return k < a.i_end ? (int)k : -1;
+    if (k >= a.i_end)
+        return -1;
+    return a.order ? a.order[k] : (int)k;
 }
 
 // true when this lane should stop taking new members (time budget spent)

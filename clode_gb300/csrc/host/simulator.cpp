@@ -191,6 +191,7 @@ struct clode_sim {
     bool buffers_single = true;
     DevBuf x0, pars, xf, rng, dt, tf, tspan_dev, odata, F, t, x, dx, aux, nstored, status, stats, stage, work;
     DevBuf ev_t, ev_x, ev_dx, ev_aux, nevents;  // features with storage: event states
+    DevBuf order, order_scratch;                // persistent kernels: members by decreasing time span
 
     // program
     bool built = false;
@@ -236,6 +237,8 @@ struct clode_sim {
     double time_budget_ms = 0.0;
     bool fuse_init = false;  // separate initialisation launch, as the reference (CLODEfeatures.cpp:180-259)
     bool collect_stats = true;
+    bool order_by_span = true;  // persistent kernels take the longest per-member time spans first
+    bool order_valid = false;   // `order` holds the permutation of the current per-member spans
     long long range_end = -1;  // autotuner trials: run members [0, range_end) only
     int range_stride = 1;      // ... every range_stride-th of them (persistent kernels)
 
@@ -267,7 +270,7 @@ struct clode_sim {
     {
         return {&x0,  &pars,   &xf,    &rng,    &dt,   &tf,    &tspan_dev, &odata, &F,
                 &t,   &x,      &dx,    &aux,    &nstored, &status, &stats, &stage, &work,
-                &ev_t, &ev_x, &ev_dx, &ev_aux, &nevents};
+                &ev_t, &ev_x, &ev_dx, &ev_aux, &nevents, &order, &order_scratch};
     }
 
     size_t real_size() const { return single ? sizeof(float) : sizeof(double); }
@@ -609,6 +612,7 @@ struct clode_sim {
         traj_rows = -1;
         events_valid = false;
         ev_rows_alloc = -1;  // event buffers are re-made for the new size or precision
+        order_valid = false;
         observer_initialized = false;
         if (tspan_per_member && (long long)tspan_pm.size() != 2 * n) {
             tspan_per_member = false;
@@ -733,6 +737,33 @@ struct clode_sim {
         return a;
     }
 
+    // Members by decreasing time span (stable), so the persistent lanes take
+    // the longest members first and the launch does not end on one lane
+    // stepping through a long member after the rest have finished (longest
+    // processing time first).  Each member's arithmetic is unchanged.
+    const int *member_order()
+    {
+        if (!(schedule == 1 && order_by_span && tspan_per_member) || nPts <= 1)
+            return nullptr;
+        if (!order_valid) {
+            size_t scratch = 0;
+            if (single)
+                order_by_span_f32(tspan_dev.as<float>(), (size_t)nPts, nullptr, nullptr, &scratch, stream);
+            else
+                order_by_span_f64(tspan_dev.as<double>(), (size_t)nPts, nullptr, nullptr, &scratch, stream);
+            order.reserve((size_t)nPts * sizeof(int));
+            order_scratch.reserve(scratch);
+            if (single)
+                order_by_span_f32(tspan_dev.as<float>(), (size_t)nPts, order.as<int>(), order_scratch.p, &scratch,
+                                  stream);
+            else
+                order_by_span_f64(tspan_dev.as<double>(), (size_t)nPts, order.as<int>(), order_scratch.p, &scratch,
+                                  stream);
+            order_valid = true;
+        }
+        return order.as<int>();
+    }
+
     // grid schedule: one thread per member.  persistent schedule: as many
     // resident blocks as the SMs hold (or blocks_per_sm per SM), lanes pull
     // members from a counter; never more threads than members.
@@ -761,15 +792,18 @@ struct clode_sim {
         }
         last_grid = (int)grid;
         last_block = (int)block;
+        const int *ord = k == kpersist ? member_order() : nullptr;
         if (single) {
             ArgsT<float> a = make_args<float>();
             a.fused_init = fused_init;
+            a.order = ord;
             void *params[] = {&a};
             check_cuda(cudaLaunchKernel((const void *)k, dim3(grid), dim3(block), params, 0, stream), "kernel launch");
             count_launch();
         } else {
             ArgsT<double> a = make_args<double>();
             a.fused_init = fused_init;
+            a.order = ord;
             void *params[] = {&a};
             check_cuda(cudaLaunchKernel((const void *)k, dim3(grid), dim3(block), params, 0, stream), "kernel launch");
             count_launch();
@@ -805,6 +839,7 @@ struct clode_sim {
 
     void sync_tspan_device()
     {
+        order_valid = false;
         if (!tspan_per_member)
             return;
         tspan_dev.reserve(std::max<size_t>(1, tspan_pm.size()) * real_size());
@@ -1054,6 +1089,7 @@ struct clode_sim {
             if (ops[k] == CLODE_OP_TRAJECTORY)
                 resize_trajectory();
         }
+        member_order();  // uploaded before any capture; replays read it in place
         bool obs_init = observer_initialized;
         if (collect_stats && nPts > 0)
             check_cuda(cudaMemsetAsync(stats.p, 0, CLODE_STAT_COUNT * sizeof(unsigned long long), stream),
@@ -1063,6 +1099,7 @@ struct clode_sim {
             std::ostringstream key;
             key << built_key << "|" << nPts << "|" << tspan[0] << "," << tspan[1] << "|" << tspan_per_member << "|"
                 << schedule << "," << block_size << "," << blocks_per_sm << "," << time_budget_ms << "," << fuse_init
+                << "," << order_by_span
                 << "|" << obs_init
                 << "|" << collect_stats << "|" << sp.dt << "," << sp.dtmax << "," << sp.abstol << "," << sp.reltol
                 << "," << sp.max_steps << "," << sp.max_store << "," << sp.nout << "|" << op.e_var_ix << ","
@@ -1906,6 +1943,8 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
             sim->fuse_init = value != 0.0;
         } else if (k == "collect_stats") {
             sim->collect_stats = value != 0.0;
+        } else if (k == "order_by_span") {
+            sim->order_by_span = value != 0.0;
         } else {
             fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);
         }
@@ -1932,6 +1971,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "time_budget_ms") *value = sim->time_budget_ms;
         else if (k == "fuse_init") *value = sim->fuse_init;
         else if (k == "collect_stats") *value = sim->collect_stats;
+        else if (k == "order_by_span") *value = sim->order_by_span;
         else if (k == "last_grid") *value = sim->last_grid;
         else if (k == "last_block") *value = sim->last_block;
         else fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);

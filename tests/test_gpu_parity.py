@@ -273,6 +273,25 @@ def test_stochastic_bitwise_rng_state(single, schedule):
         np.testing.assert_allclose(eng["xf"], s.get_xf(), rtol=1e-9, atol=1e-12)
 
 
+@pytest.mark.parametrize("fuse", [0, 1])
+def test_longest_span_first_order_changes_nothing(fuse):
+    # the persistent lanes take members in decreasing order of their time
+    # span by default; every member's results must equal those of the
+    # natural order bit for bit
+    n = 3000
+    rng = np.random.default_rng(8)
+    pars = np.stack([rng.uniform(0.5, 3.0, n), np.full(n, 3.0), rng.uniform(0.0, 2.0, n)], axis=1)
+    x0 = np.tile([-60.0, 0.0, 0.0, 0.1], (n, 1))
+    tspan = np.stack([np.zeros(n), rng.uniform(200.0, 2000.0, n)], axis=1)
+    sc = Scenario("lactotroph.cl", 4, 3, x0, pars, n_aux=1, stepper="dopri5", single=True,
+                  observer="nhood2", op=dict(e_var_ix=3, f_var_ix=0), tspan_pm=tspan, steps=[("features", None, True)])
+    runs = [run_engine(sc, options={"schedule": 1, "fuse_init": fuse, "order_by_span": o}) for o in (0, 1)]
+    for k in ("xf", "tf", "dt"):
+        assert np.array_equal(runs[0][k], runs[1][k], equal_nan=True), k
+    assert np.array_equal(runs[0]["F_list"][0], runs[1]["F_list"][0], equal_nan=True)
+    assert runs[0]["stats"] == runs[1]["stats"]
+
+
 def test_all_zero_rng_state_is_rejected():
     # (0, 0) is xoroshiro128+'s fixed point: the polar method would reject
     # every candidate drawn from it, so such a state is refused on the host
