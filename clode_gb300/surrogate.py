@@ -239,8 +239,23 @@ class FeatureMapScreen:
         sy = np.unique(np.r_[0:ny:train_stride, ny - 1])
         SX, SY = np.meshgrid(sx, sy, indexing="xy")
         sub = (SY * nx + SX).ravel()
+        # the calibration sample (random interior points, used in step 5) is
+        # drawn now and integrated in the same engine call as the sub-grid:
+        # one large launch instead of a second small one
+        is_sub = np.zeros(nx * ny, dtype=bool)
+        is_sub[sub] = True
+        rng = np.random.default_rng(self.seed + 101)
+        want = min(n_calibration, nx * ny - sub.size)
+        cal = np.zeros(0, dtype=np.int64)
+        while cal.size < want:
+            cand = rng.integers(0, nx * ny, size=2 * (want - cal.size) + 16)
+            cal = np.unique(np.r_[cal, cand[~is_sub[cand]]])
+        if cal.size > want:
+            cal = rng.choice(cal, size=want, replace=False)
         t0 = time.perf_counter()
-        Fsub = np.asarray(self.integrate(g0[SX.ravel()], g1[SY.ravel()]), dtype=np.float64)
+        Fboth = np.asarray(self.integrate(np.r_[g0[SX.ravel()], g0[cal % nx]], np.r_[g1[SY.ravel()], g1[cal // nx]]),
+                           dtype=np.float64)
+        Fsub, Fcal = Fboth[:sub.size], Fboth[sub.size:]
         t_train_data = time.perf_counter() - t0
         lo, hi = Fsub.min(axis=0), Fsub.max(axis=0)
         scale = np.maximum(hi - lo, 1e-30)
@@ -280,22 +295,11 @@ class FeatureMapScreen:
         flags[sub] = ScreenResult.SAMPLED
         F[sub] = Fsub
         t_cells = time.perf_counter() - t0
-        # 5. calibration sample: random interior points, integrated exactly
+        # 5. calibration: the screen's thresholds from the sample's exact values
         t0 = time.perf_counter()
-        rng = np.random.default_rng(self.seed + 101)
-        n_int = nx * ny - sub.size
-        want = min(n_calibration, n_int)
-        cal = np.zeros(0, dtype=np.int64)
-        while cal.size < want:
-            cand = rng.integers(0, nx * ny, size=2 * (want - cal.size) + 16)
-            cand = cand[flags[cand] == ScreenResult.SURROGATE]
-            cal = np.unique(np.r_[cal, cand])
-        if cal.size > want:
-            cal = rng.choice(cal, size=want, replace=False)
         tr, tv, acc = -1.0, -1.0, 0.0
         if cal.size:
             ix, iy = cal % nx, cal // nx
-            Fcal = np.asarray(self.integrate(g0[ix], g1[iy]), dtype=np.float64)
             err_cal = self.map_error(F[cal], Fcal, scale)
             tr, tv, acc = self._calibrate(r_cell[cy[iy], cx[ix]], v_cell[cy[iy], cx[ix]], err_cal, tol, keep)
             F[cal] = Fcal
