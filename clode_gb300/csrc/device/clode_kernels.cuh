@@ -76,9 +76,10 @@ __device__ __forceinline__ void member_load(Member &m, const Args &a, int i, Cou
     m.r.s1 = a.rng[n + i];
     m.r.have_spare = false;
     m.r.spare = ZERO;
+    m.sqdt = sqrt(m.dt);
 #pragma unroll
     for (int j = 0; j < N_WIENER; ++j)
-        m.w[j] = rng_normal(m.r) / sqrt(m.dt);
+        m.w[j] = rng_normal(m.r) / m.sqdt;
 #endif
     getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
     c.rhs += 1;

@@ -34,6 +34,9 @@ struct Member {
     realtype aux[NA1];
     realtype w[NW1];
     Rng r;
+#if CLODE_STOCHASTIC
+    realtype sqdt;  // sqrt(dt), fixed for the whole launch: the stochastic stepper never changes dt
+#endif
 };
 
 // per-thread work counters, summed into ArgsT::stats at the end of a member
@@ -105,7 +108,7 @@ __device__ __forceinline__ int step_member(Member &m, const SolverParams &sp, co
 #if CLODE_STOCHASTIC
 #pragma unroll
     for (int j = 0; j < N_WIENER; ++j)
-        m.w[j] = rng_normal(m.r) / sqrt(m.dt);
+        m.w[j] = rng_normal(m.r) / m.sqdt;  // randn / sqrt(dt), fixed_explicit_step.clh:29-33
 #endif
     getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
     c.steps++;
