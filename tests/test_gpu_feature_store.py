@@ -52,17 +52,17 @@ def _setup(sim, noise, max_store, nout, options):
         sim.seed_rng(99)
 
 
-def _features_sim(noise, max_store, nout, options, nse=5):
+def _features_sim(noise, max_store, nout, options, nse=5, single=True):
     sim = W.FeatureSimulatorBase(_problem(noise), "seuler" if noise else "dopri5", "nhood2",
                                  W.ObserverParams(e_var_ix=3, f_var_ix=0, max_event_timestamps=nse,
                                                   nhood_radius=0.05, max_event_count=100000),
-                                 True, W.OpenCLResource(), "")
+                                 single, W.OpenCLResource(), "")
     _setup(sim, noise, max_store, nout, options)
     return sim
 
 
-def _trajectory_sim(noise, max_store, nout, options):
-    sim = W.TrajectorySimulatorBase(_problem(noise), "seuler" if noise else "dopri5", True, W.OpenCLResource(), "")
+def _trajectory_sim(noise, max_store, nout, options, single=True):
+    sim = W.TrajectorySimulatorBase(_problem(noise), "seuler" if noise else "dopri5", single, W.OpenCLResource(), "")
     _setup(sim, noise, max_store, nout, {k: v for k, v in options.items() if k != "fuse_init"})
     return sim
 
@@ -105,6 +105,25 @@ def test_store_run_equals_features_and_trajectory(noise, schedule, fuse):
         have = n_ev > k
         assert _same(et[k, have], F[names.index(f"nhood event time {k}"), have]), k
         assert (et[k, ~have] == 0).all()
+
+
+def test_store_run_fp64():
+    options = {"schedule": 1}
+    plain = _features_sim(False, 8000, 20, options, single=False)
+    plain.features(True)
+    store = _features_sim(False, 8000, 20, options, single=False)
+    store.features_store(True, event_rows=4)
+    assert _same(store.get_f(), plain.get_f()) and _same(store.get_xf(), plain.get_xf())
+    traj = _trajectory_sim(False, 8000, 20, options, single=False)
+    traj.trajectory()
+    assert _same(store.get_n_stored(), traj.get_n_stored())
+    for get in ("get_t", "get_x", "get_dx", "get_aux"):
+        assert _same(getattr(store, get)(), getattr(traj, get)()), get
+    by_member = store.get_trajectory_by_member(first=3, count=9)
+    ns = traj.get_n_stored()[3:12]
+    t_flat = traj.get_t().reshape(8000, N)[:, 3:12].T
+    for i in range(9):
+        assert _same(by_member["t"][i, :ns[i] + 1], t_flat[i, :ns[i] + 1])
 
 
 def test_event_states_lie_on_the_trajectory():
