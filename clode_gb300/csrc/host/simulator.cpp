@@ -1611,7 +1611,13 @@ int clode_sim_set_observer(clode_sim *sim, const char *observer)
         sim->set_observer(observer);
     });
 }
-int clode_sim_build(clode_sim *sim) { SIM_GUARD(sim->build()); }
+int clode_sim_build(clode_sim *sim)
+{
+    SIM_GUARD({
+        sim->want_store = false;  // the plain program (CLODE::buildCL); features_store builds its own
+        sim->build();
+    });
+}
 
 int clode_sim_set_problem_data(clode_sim *sim, const double *x0, size_t n_x0, const double *pars, size_t n_pars)
 {
@@ -2021,6 +2027,9 @@ void noalloc_features_prepare(clode_sim *sim, NoallocFeaturesLaunch *out)
         fail(CLODE_ERR_NOT_BUILT, "the feature simulator must be built (clode_sim_build) on its device first");
     if (!sim->observer_program_current())
         fail(CLODE_ERR_NOT_BUILT, "observer parameters changed the program: rebuild with clode_sim_build");
+    if (sim->built_store)
+        fail(CLODE_ERR_NOT_BUILT, "the loaded program stores trajectories (features_store ran last): rebuild the plain "
+                                  "program with clode_sim_build");
     memset(out, 0, sizeof *out);
     out->kernel = (void *)sim->kp_features;
     out->single = sim->single ? 1 : 0;

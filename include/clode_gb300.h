@@ -341,7 +341,8 @@ unsigned long long clode_launch_count(void);
  * default stream) and the call returns without waiting; every call shares the
  * one array, so calls that overlap on the GPU race and must be ordered by the
  * caller.  The simulator must be a feature simulator built on its device
- * (clode_sim_build) after its last observer-parameter change. */
+ * (clode_sim_build) after its last observer-parameter change and after its
+ * last clode_sim_features_store (which loads a program that stores rows). */
 int clode_sim_features_noalloc(clode_sim *sim, long long n_pts, const void *x0, const void *pars,
                                const void *tspan, unsigned long long *rng, void *dt, void *xf, void *tf,
                                void *F, int *status, void *stream);

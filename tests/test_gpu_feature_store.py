@@ -208,3 +208,17 @@ def test_features_after_store_run_is_plain_features():
         sim.set_solver_params(W.SolverParams(dt=0.1, dtmax=1.0, abstol=1e-6, reltol=1e-6, max_steps=1000,
                                              max_store=10, nout=0))
         sim.features_store(True)
+
+
+def test_noalloc_refuses_the_store_program():
+    # the allocation-free entry point runs the plain features kernel only: after
+    # a features_store run it asks for the plain program to be rebuilt first
+    import ctypes as C
+    from clode_gb300 import _native as Nt
+    sim = _features_sim(False, 500, 20, {"schedule": 1})
+    sim.features_store(True, event_rows=2)
+    rc = Nt.lib.clode_sim_features_noalloc(sim._handle, 0, None, None, None, None, None, None, None, None, None, None)
+    assert rc == 4  # CLODE_ERR_NOT_BUILT
+    sim.build_cl()
+    rc = Nt.lib.clode_sim_features_noalloc(sim._handle, 0, None, None, None, None, None, None, None, None, None, None)
+    assert rc == 0  # n_pts = 0: nothing to launch
