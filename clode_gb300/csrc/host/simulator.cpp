@@ -1081,6 +1081,7 @@ struct clode_sim {
     void chain(const int *ops, int n, bool use_graph)
     {
         require_problem();
+        want_store = false;  // chained features ops run the plain program
         ensure_built();
         ensure_stream();
         for (int k = 0; k < n; ++k) {  // every allocation happens before any capture
@@ -1160,6 +1161,7 @@ struct clode_sim {
     void autotune(long long sample, double *best_ms_out)
     {
         require_problem();
+        want_store = false;  // tunes (and leaves loaded) the plain program
         long long S = std::min(nPts, sample > 0 ? sample : nPts);
         if (S <= 0)
             fail(CLODE_ERR_STATE, "no members to tune on");
