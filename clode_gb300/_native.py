@@ -122,6 +122,8 @@ SIGNATURES = {
     "clode_sim_features_store": (C.c_int, [_P, C.c_int, C.c_uint]),
     "clode_sim_get_n_events": (C.c_int, [_P, C.POINTER(C.c_int), _SIZE, C.POINTER(_SIZE)]),
     "clode_sim_set_store_variables": (C.c_int, [_P, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int]),
+    "clode_sim_get_events_by_member": (C.c_int, [_P, C.c_longlong, C.c_longlong, C.c_longlong, _DP, _DP, _DP, _DP,
+                                                 C.POINTER(C.c_int)]),
     "clode_sim_get_trajectory_by_member": (C.c_int, [_P, C.c_longlong, C.c_longlong, C.c_longlong, _DP, _DP, _DP,
                                                      _DP, C.POINTER(C.c_int)]),
     "clode_sim_get_rng_state": (C.c_int, [_P, C.POINTER(C.c_ulonglong), _SIZE, C.POINTER(_SIZE)]),

@@ -709,16 +709,19 @@ class _StoredRows:
         stored trajectory among those members; ``which`` selects the arrays
         to fetch ("aux" is omitted when the model has none).
         """
+        return self._by_member(N.lib.clode_sim_get_trajectory_by_member, "n_stored", 1, first, count, rows, which,
+                               lambda s: int(s.max_store))
+
+    def _by_member(self, fn, counts_key: str, extra_row: int, first, count, rows, which, max_rows) -> dict:
         s = N.CSizes()
         _check(N.lib.clode_sim_get_sizes(self._handle, C.byref(s)))
         n_pts, n_var, n_aux = int(s.n_pts), int(s.n_store_var), int(s.n_store_aux)
         count = n_pts - first if count is None else int(count)
         ns = np.zeros(max(count, 0), dtype=np.int32)
-        _check(N.lib.clode_sim_get_trajectory_by_member(self._handle, first, count, 0, None, None, None, None,
-                                                         ns.ctypes.data_as(C.POINTER(C.c_int))))
+        _check(fn(self._handle, first, count, 0, None, None, None, None, ns.ctypes.data_as(C.POINTER(C.c_int))))
         if rows is None:
-            rows = min(int(s.max_store), int(ns.max()) + 1) if count > 0 else 0
-        out = {"n_stored": ns}
+            rows = min(max_rows(s), int(ns.max()) + extra_row) if count > 0 else 0
+        out = {counts_key: ns}
         shapes = {"t": (count, rows), "x": (count, rows, n_var), "dx": (count, rows, n_var),
                   "aux": (count, rows, n_aux)}
         ptrs = []
@@ -728,7 +731,7 @@ class _StoredRows:
                 ptrs.append(N.dptr(out[k]))
             else:
                 ptrs.append(None)
-        _check(N.lib.clode_sim_get_trajectory_by_member(self._handle, first, count, rows, *ptrs, None))
+        _check(fn(self._handle, first, count, rows, *ptrs, None))
         return out
 
 
@@ -789,6 +792,16 @@ class FeatureSimulatorBase(SimulatorBase, _StoredRows):
 
     def get_event_aux(self) -> np.ndarray:
         return self._get(N.ARRAY_EVENT_AUX)
+
+    def get_events_by_member(self, first: int = 0, count: Optional[int] = None, rows: Optional[int] = None,
+                             which=("t", "x", "dx", "aux")) -> dict:
+        """The event states of the last ``features_store`` regrouped by member
+        (addition): ``{"n_events": (count,), "t": (count, rows), "x": (count,
+        rows, nVar), ...}``; member i's events are ``t[i, :min(n_events[i],
+        rows)]``.  ``rows`` defaults to the most events any of these members
+        stored."""
+        return self._by_member(N.lib.clode_sim_get_events_by_member, "n_events", 0, first, count, rows, which,
+                               lambda s: int(s.event_rows))
 
     def get_n_events(self) -> np.ndarray:
         n = C.c_size_t(0)

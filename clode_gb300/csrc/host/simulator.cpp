@@ -1376,33 +1376,37 @@ struct clode_sim {
     }
 
     // Rows [0, rows) of members [first, first + count) of the last
-    // trajectory, regrouped member-major on the device (one transpose per
-    // stored array, see launch_regroup_by_member_*) and copied out in chunks
-    // of at most 256 MB of staging.  Null outputs are skipped.
-    void get_by_member(long long first, long long count, long long rows, double *t_out, double *x_out,
-                       double *dx_out, double *aux_out, int *nstored_out)
+    // trajectory (events == false) or of the last run's event states
+    // (events == true), regrouped member-major on the device (one transpose
+    // per stored array, see launch_regroup_by_member_*) and copied out in
+    // chunks of at most 256 MB of staging.  Null outputs are skipped.
+    void get_by_member(bool events, long long first, long long count, long long rows, double *t_out, double *x_out,
+                       double *dx_out, double *aux_out, int *counts_out)
     {
-        if (traj_rows <= 0)
-            fail(CLODE_ERR_INVALID_ARGUMENT, "no trajectory has been run");
+        if (events ? !events_valid : traj_rows <= 0)
+            fail(CLODE_ERR_INVALID_ARGUMENT, events ? "no run has stored event states" : "no trajectory has been run");
         if (first < 0 || count < 0 || first + count > nPts)
             fail(CLODE_ERR_INVALID_ARGUMENT, "members [%lld, %lld) are outside [0, %lld)", first, first + count,
                  nPts);
-        if (rows < 0 || rows > (long long)stored_rows())
-            fail(CLODE_ERR_INVALID_ARGUMENT, "rows = %lld is outside [0, %zu] (max_store of the stored run)", rows,
-                 stored_rows());
+        const size_t max_rows = events ? (size_t)ev_rows : stored_rows();
+        if (rows < 0 || rows > (long long)max_rows)
+            fail(CLODE_ERR_INVALID_ARGUMENT, "rows = %lld is outside [0, %zu] (rows of the stored run)", rows,
+                 max_rows);
         if (!count)
             return;
         ensure_stream();
-        if (nstored_out)
-            check_cuda(cudaMemcpyAsync(nstored_out, nstored.as<int>() + first, (size_t)count * sizeof(int),
-                                       cudaMemcpyDeviceToHost, stream),
+        if (counts_out)
+            check_cuda(cudaMemcpyAsync(counts_out, (events ? nevents : nstored).as<int>() + first,
+                                       (size_t)count * sizeof(int), cudaMemcpyDeviceToHost, stream),
                        "D2H copy");
         struct Part {
             const DevBuf *src;
             double *out;
             size_t width;
-        } parts[4] = {{&t, t_out, 1}, {&x, x_out, (size_t)store_nv()}, {&dx, dx_out, (size_t)store_nv()},
-                      {&aux, aux_out, (size_t)store_na()}};
+        } parts[4] = {{events ? &ev_t : &t, t_out, 1},
+                      {events ? &ev_x : &x, x_out, (size_t)store_nv()},
+                      {events ? &ev_dx : &dx, dx_out, (size_t)store_nv()},
+                      {events ? &ev_aux : &aux, aux_out, (size_t)store_na()}};
         const size_t stage_max = (size_t)256 << 20;
         for (const Part &p : parts) {
             if (!p.out || p.width == 0 || rows == 0)
@@ -1774,7 +1778,13 @@ int clode_sim_get_trajectory_by_member(clode_sim *sim, long long first, long lon
                                        double *t_out, double *x_out, double *dx_out, double *aux_out,
                                        int *n_stored_out)
 {
-    SIM_GUARD({ sim->get_by_member(first, count, rows, t_out, x_out, dx_out, aux_out, n_stored_out); });
+    SIM_GUARD({ sim->get_by_member(false, first, count, rows, t_out, x_out, dx_out, aux_out, n_stored_out); });
+}
+
+int clode_sim_get_events_by_member(clode_sim *sim, long long first, long long count, long long rows, double *t_out,
+                                   double *x_out, double *dx_out, double *aux_out, int *n_events_out)
+{
+    SIM_GUARD({ sim->get_by_member(true, first, count, rows, t_out, x_out, dx_out, aux_out, n_events_out); });
 }
 
 int clode_sim_features_store(clode_sim *sim, int initialize_observer, unsigned int event_rows)

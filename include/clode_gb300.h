@@ -265,6 +265,13 @@ int clode_sim_get_trajectory_by_member(clode_sim *sim, long long first, long lon
 int clode_sim_features_store(clode_sim *sim, int initialize_observer, unsigned int event_rows);
 /* Events each member met in the feature pass of the last clode_sim_features_store() */
 int clode_sim_get_n_events(clode_sim *sim, int *out, size_t capacity, size_t *n);
+/* The event states of the last clode_sim_features_store() regrouped by member,
+ * as clode_sim_get_trajectory_by_member() does for rows (rows <= event_rows):
+ * t_out[(i - first) * rows + k], x_out[((i - first) * rows + k) * n + j], ...,
+ * n_events_out[i - first].  Member i's events are its first
+ * min(n_events, rows) rows; the rest read zero. */
+int clode_sim_get_events_by_member(clode_sim *sim, long long first, long long count, long long rows, double *t_out,
+                                   double *x_out, double *dx_out, double *aux_out, int *n_events_out);
 /* Stored columns of trajectories and event states: the variables var_ix[0..n_var_ix)
  * and auxiliary variables aux_ix[0..n_aux_ix), in that order (the option
  * clode/cpp/trajectory.cl:3 leaves as a TODO).  A negative count keeps all of

@@ -222,3 +222,22 @@ def test_noalloc_refuses_the_store_program():
     sim.build_cl()
     rc = Nt.lib.clode_sim_features_noalloc(sim._handle, 0, None, None, None, None, None, None, None, None, None, None)
     assert rc == 0  # n_pts = 0: nothing to launch
+
+
+def test_events_by_member_match_the_flat_arrays():
+    from oracle.trajectory_frontend import regroup_by_member
+    ev_rows = 6
+    store = _features_sim(False, 4000, 20, {"schedule": 1})
+    store.features_store(True, event_rows=ev_rows)
+    n_ev = store.get_n_events()
+    got = store.get_events_by_member()
+    rows = got["t"].shape[1]
+    assert rows == min(ev_rows, int(n_ev.max()))
+    assert np.array_equal(got["n_events"], n_ev)
+    for k, w in (("t", 1), ("x", 4), ("dx", 4), ("aux", 1)):
+        flat = getattr(store, "get_event_" + k)()
+        want = regroup_by_member(flat, N, w, 0, N, rows)
+        assert _same(got[k].reshape(N, rows, w), want), k
+    part = store.get_events_by_member(first=100, count=20, rows=ev_rows)
+    assert part["t"].shape == (20, ev_rows)
+    assert _same(part["t"], regroup_by_member(store.get_event_t(), N, 1, 100, 20, ev_rows)[:, :, 0])
