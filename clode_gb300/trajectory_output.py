@@ -97,3 +97,31 @@ def get_trajectory(sim, variable_names: Optional[List[str]] = None, aux_names: O
         for i, n in enumerate((ns + 1).tolist())
     ]
     return results[0] if len(results) == 1 else results
+
+
+def trajectory_chunks(sim, t_span, n_chunks: int, update_x0: bool = True):
+    """A long trajectory as ``n_chunks`` consecutive runs over equal parts of
+    ``t_span``, so the stored rows of one part at a time fill the device
+    buffers (max_store rows per part).  clODE leaves this as a TODO
+    (clode/trajectory.py:166: "chunk time - keep max_store to a reasonable
+    level, loop solve/get until t_span is covered").
+
+    Each chunk is exactly what a clODE user gets from
+    ``TrajectorySimulator.trajectory(t_span=part, update_x0=True)``: the
+    trajectory kernel over the part, then ``shift_x0`` so the next part
+    starts from the final state (the step size and the RNG stream continue;
+    the cached second normal deviate is dropped at every launch, as in the
+    reference).  Yields, per chunk, ``(t0, t1, rows)`` with ``rows`` the
+    member-major arrays of ``get_trajectory_by_member``.
+    """
+    a, b = float(t_span[0]), float(t_span[1])
+    if n_chunks < 1:
+        raise ValueError("n_chunks must be at least 1")
+    edges = [a + (b - a) * k / n_chunks for k in range(n_chunks)] + [b]
+    for k in range(n_chunks):
+        sim.set_tspan([edges[k], edges[k + 1]])
+        sim.trajectory()
+        rows = sim.get_trajectory_by_member()
+        if update_x0:
+            sim.shift_x0()
+        yield edges[k], edges[k + 1], rows

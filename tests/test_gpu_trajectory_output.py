@@ -110,3 +110,32 @@ def test_getters_stay_within_the_stored_run():
         sim.get_trajectory_by_member(rows=51)
     sim.trajectory()
     assert sim.get_t().size == 500 * 40
+
+
+def test_trajectory_chunks_equal_the_repeated_calls():
+    # the chunked helper against the calls a clODE user makes by hand:
+    # trajectory over each part, then shift_x0
+    from clode_gb300.trajectory_output import trajectory_chunks
+
+    def make():
+        pi = W.ProblemInfo(rhs_path("ornstein_uhlenbeck.cl"), ["x"], ["theta", "mu", "sigma"], [], 1)
+        sim = W.TrajectorySimulatorBase(pi, "seuler", True, W.OpenCLResource(), "")
+        n = 512
+        rng = np.random.default_rng(9)
+        pars = np.stack([rng.uniform(0.1, 2.0, n), np.zeros(n), rng.uniform(0.1, 1.0, n)], axis=1)
+        sim.set_solver_params(W.SolverParams(dt=1e-3, max_steps=100000, max_store=205, nout=10))
+        sim.set_problem_data(np.zeros(n), pars.flatten(order="F"))
+        sim.seed_rng(4)
+        return sim
+
+    a, b = make(), make()
+    got = list(trajectory_chunks(a, (0.0, 6.0), 3))
+    assert [(t0, t1) for t0, t1, _ in got] == [(0.0, 2.0), (2.0, 4.0), (4.0, 6.0)]
+    for t0, t1, rows in got:
+        b.set_tspan([t0, t1])
+        b.trajectory()
+        want = b.get_trajectory_by_member()
+        b.shift_x0()
+        for k in ("n_stored", "t", "x", "dx"):
+            assert np.array_equal(rows[k], want[k]), k
+    assert np.array_equal(a.get_xf(), b.get_xf()) and np.array_equal(a.get_rng_state(), b.get_rng_state())
