@@ -46,9 +46,9 @@ FLOPS_PER_ATTEMPT = 62 * N_VAR + 10   # DP45 stage combinations and error norm
 FLOPS_PER_STEP_OBS = 5 * N_VAR + 3 * N_AUX + 6  # nhood2 per-step extrema and means
 # DRAM bytes (read + write) per member of one map (warm-up launch + feature
 # launch): ncu dram__bytes_{read,write}.sum of both launches of the default
-# build on the 512 x 512 case (262,144 members: 136.3 MB + 2341.5 MB), scaled
+# build on the 512 x 512 case (262,144 members: 76.6 MB + 519.6 MB), scaled
 # by members; the traffic is per-member state, so it grows in proportion
-DRAM_BYTES_PER_MEMBER = (67184384 + 69066240 + 1388177408 + 953297920) / 262144
+DRAM_BYTES_PER_MEMBER = (36643072 + 39959552 + 216447488 + 303181824) / 262144
 
 
 def make_workload(grid: int, seed: int, tmin: float, tmax: float, rank: int = 0):

@@ -404,28 +404,35 @@ extern "C" __global__ void clode_trajectory_persistent(const Args a)
 // --------------------------------------------------- parked observer state --
 static_assert(sizeof(Observer) % 4 == 0, "observer state must be a whole number of 32-bit words");
 #define CLODE_OBS_WORDS ((int)(sizeof(Observer) / 4))
+// Parked state is member-major, [i * CLODE_OBS_STRIDE + word], each member's
+// words rounded up to whole 16-byte vectors: a lane moves its member's state
+// in contiguous 16-byte pieces, so every sector it touches is written (or
+// read) whole, whatever order the members are taken in.
+#define CLODE_OBS_VEC ((CLODE_OBS_WORDS + 3) / 4)
+#define CLODE_OBS_STRIDE (4 * CLODE_OBS_VEC)
 
-// read by the host to size the parked-state buffer
-extern "C" __device__ const unsigned int clode_observer_words = CLODE_OBS_WORDS;
+// read by the host to size the parked-state buffer (words per member, padding included)
+extern "C" __device__ const unsigned int clode_observer_words = CLODE_OBS_STRIDE;
 
 __device__ __forceinline__ void park_load(Observer &o, const Args &a, int i)
 {
-    const unsigned long long n = (unsigned long long)a.nPts;
-    unsigned int w[CLODE_OBS_WORDS];
+    const uint4 *src = reinterpret_cast<const uint4 *>(a.odata + (unsigned long long)i * CLODE_OBS_STRIDE);
+    uint4 v[CLODE_OBS_VEC];
 #pragma unroll
-    for (int k = 0; k < CLODE_OBS_WORDS; ++k)
-        w[k] = a.odata[k * n + i];
-    memcpy(&o, w, sizeof(Observer));
+    for (int k = 0; k < CLODE_OBS_VEC; ++k)
+        v[k] = src[k];
+    memcpy(&o, v, sizeof(Observer));
 }
 
 __device__ __forceinline__ void park_store(const Observer &o, const Args &a, int i)
 {
-    const unsigned long long n = (unsigned long long)a.nPts;
-    unsigned int w[CLODE_OBS_WORDS];
-    memcpy(w, &o, sizeof(Observer));
+    uint4 *dst = reinterpret_cast<uint4 *>(a.odata + (unsigned long long)i * CLODE_OBS_STRIDE);
+    uint4 v[CLODE_OBS_VEC];
+    v[CLODE_OBS_VEC - 1] = make_uint4(0u, 0u, 0u, 0u);
+    memcpy(v, &o, sizeof(Observer));
 #pragma unroll
-    for (int k = 0; k < CLODE_OBS_WORDS; ++k)
-        a.odata[k * n + i] = w[k];
+    for (int k = 0; k < CLODE_OBS_VEC; ++k)
+        dst[k] = v[k];
 }
 
 // Observer initialisation for one member (initializeObserver.cl:9-84).

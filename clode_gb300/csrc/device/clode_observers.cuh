@@ -1,8 +1,9 @@
 // On-the-fly feature observers.  One observer is compiled in per program
 // (USE_OBSERVER_*).  Its state is a plain struct held in registers for the
-// whole time loop; between launches it is parked in global memory as 32-bit
-// words in SoA order ([word * nPts + member]) so that loads and stores
-// coalesce across a warp.  That layout is private to this engine; only the
+// whole time loop; between launches it is parked in global memory
+// member-major in 16-byte vectors ([member * stride + word], see park_store),
+// so a lane moves its member's state in whole sectors whichever members its
+// warp holds.  That layout is private to this engine; only the
 // feature vector F has a public layout (F[k * nPts + i], k in the order of
 // the reference's feature-name lists).
 //
