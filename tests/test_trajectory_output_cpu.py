@@ -121,3 +121,36 @@ def test_views_share_memory():
     integ = FakeIntegrator(8, 2, 1, 6)
     outs = get_trajectory(integ)
     assert outs[1].x.base is not None and np.shares_memory(outs[1].x, outs[2].x.base)
+
+
+def test_trajectory_chunks_call_sequence():
+    from clode_gb300.trajectory_output import trajectory_chunks
+
+    class Sim:
+        def __init__(self):
+            self.calls = []
+
+        def set_tspan(self, ts):
+            self.calls.append(("tspan", tuple(ts)))
+
+        def trajectory(self):
+            self.calls.append(("trajectory",))
+
+        def get_trajectory_by_member(self):
+            self.calls.append(("get",))
+            return {"n_stored": np.zeros(1, dtype=np.int32)}
+
+        def shift_x0(self):
+            self.calls.append(("shift_x0",))
+
+    s = Sim()
+    chunks = list(trajectory_chunks(s, (1.0, 4.0), 3))
+    assert [c[:2] for c in chunks] == [(1.0, 2.0), (2.0, 3.0), (3.0, 4.0)]
+    assert s.calls == [("tspan", (1.0, 2.0)), ("trajectory",), ("get",), ("shift_x0",),
+                       ("tspan", (2.0, 3.0)), ("trajectory",), ("get",), ("shift_x0",),
+                       ("tspan", (3.0, 4.0)), ("trajectory",), ("get",), ("shift_x0",)]
+    s2 = Sim()
+    list(trajectory_chunks(s2, (0.0, 1.0), 1, update_x0=False))
+    assert ("shift_x0",) not in s2.calls
+    with pytest.raises(ValueError):
+        list(trajectory_chunks(Sim(), (0.0, 1.0), 0))
