@@ -676,6 +676,7 @@ def main():
                    "autotune": tuned, "schedule_used": int(sim.get_option("schedule")),
                    "maxrregcount": int(sim.get_option("maxrregcount")),
                    "block_size_used": int(sim.get_option("block_size")),
+                   "last_launch": {"grid": int(sim.get_option("last_grid")), "block": int(sim.get_option("last_block"))},
                    "l2": "256 MB buffer zeroed between timed steps; inputs 150 MB > L2"},
         "rhs_evals_per_s": rhs_per_s,
         "stats_per_step": st,

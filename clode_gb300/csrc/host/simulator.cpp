@@ -771,7 +771,20 @@ struct clode_sim {
     {
         if (nPts == 0)
             return;
+        int sms = 0;
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count");
         unsigned int block = (unsigned int)std::max(32, std::min(1024, block_size));
+        // Few members (fewer than one block per SM at this block size): shrink
+        // the block, in whole warps, until the blocks reach every SM.  Each
+        // member still has its own thread; its SM's pipes serve fewer warps.
+        long long active = range_end >= 0 ? std::min(range_end, nPts) : nPts;
+        if (range_stride > 1)
+            active = (active + range_stride - 1) / range_stride;
+        if ((long long)block * sms > active) {
+            const long long per_sm_members = (active + sms - 1) / std::max(sms, 1);
+            const unsigned int b = (unsigned int)std::max<long long>(32, (per_sm_members + 31) / 32 * 32);
+            block = std::min(block, b);
+        }
         unsigned int grid = (unsigned int)((nPts + block - 1) / block);
         cudaKernel_t k = kgrid;
         if (schedule == 1 && kpersist) {
@@ -782,8 +795,6 @@ struct clode_sim {
                            "occupancy query");
                 per_sm = std::max(per_sm, 1);
             }
-            int sms = 0;
-            check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count");
             unsigned long long want = (unsigned long long)per_sm * sms;
             grid = (unsigned int)std::min<unsigned long long>(want, grid);
             check_cuda(cudaMemsetAsync(work.p, 0, sizeof(unsigned int), stream), "work counter reset");
