@@ -101,6 +101,8 @@ struct ArgsT {
     // persistent kernels: position k of the range runs member order[k]
     // (null: member k), e.g. the longest time spans first
     const int *order;
+    // persistent observer initialisation: each member's warm-up steps (null: not recorded)
+    int *work_out;
     SolverParamsT<R> sp;
     ObserverParamsT<R> op;
 };

@@ -529,6 +529,8 @@ extern "C" __global__ void clode_init_observer_persistent(const Args a)
             }
             o.arm(m.t, m.x, m.dx, m.aux, a.op);
             park_store(o, a, i);
+            if (a.work_out)  // the feature pass repeats these steps: the host orders it by them
+                a.work_out[i] = (int)step;
             i = -1;
         }
     }

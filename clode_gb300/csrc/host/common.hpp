@@ -96,6 +96,8 @@ void launch_fill_i32(int *dst, int v, size_t n, cudaStream_t s);
 // device): with scratch == NULL only *scratch_bytes is set
 void order_by_span_f32(const float *tspan, size_t n, int *order, void *scratch, size_t *scratch_bytes, cudaStream_t s);
 void order_by_span_f64(const double *tspan, size_t n, int *order, void *scratch, size_t *scratch_bytes, cudaStream_t s);
+// Members by decreasing count (counts[i] >= 0), same conventions
+void order_by_count(const int *counts, size_t n, int *order, void *scratch, size_t *scratch_bytes, cudaStream_t s);
 // dst[(i - m0) * nc + c] = src[c * ld + i] for members i in [m0, m0 + nm), c < nc
 void launch_regroup_by_member_f32(const float *src, size_t ld, size_t m0, size_t nm, size_t nc, double *dst,
                                   cudaStream_t s);

@@ -48,7 +48,45 @@ void order_impl(const T *tspan, size_t n, int *order, void *scratch, size_t *scr
                "member order sort");
 }
 
+__global__ void k_iota(size_t n, int *__restrict__ idx)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        idx[i] = (int)i;
+}
+
 }  // namespace
+
+// Members by decreasing count (non-negative ints, e.g. warm-up steps); the
+// same scratch layout as the span order
+void order_by_count(const int *counts, size_t n, int *order, void *scratch, size_t *scratch_bytes, cudaStream_t s)
+{
+    const size_t keys_bytes = (n * sizeof(unsigned int) + 255) & ~(size_t)255;
+    const size_t idx_bytes = (n * sizeof(int) + 255) & ~(size_t)255;
+    size_t temp = 0;
+    check_cuda(cub::DeviceRadixSort::SortPairsDescending(nullptr, temp, (const unsigned int *)nullptr,
+                                                        (unsigned int *)nullptr, (const int *)nullptr, (int *)nullptr,
+                                                        (int)n, 0, 32, s),
+               "member order sort size");
+    const size_t need = keys_bytes + idx_bytes + temp;
+    if (!scratch) {
+        *scratch_bytes = need;
+        return;
+    }
+    if (*scratch_bytes < need)
+        fail(CLODE_ERR_INTERNAL, "member order scratch too small");
+    unsigned char *p = (unsigned char *)scratch;
+    unsigned int *keys_out = (unsigned int *)p;
+    int *idx_in = (int *)(p + keys_bytes);
+    void *tmp = p + keys_bytes + idx_bytes;
+    const unsigned int grid = (unsigned int)std::min<size_t>((n + 255) / 256, 4864);
+    k_iota<<<grid, 256, 0, s>>>(n, idx_in);
+    count_launch();
+    check_cuda(cudaGetLastError(), "member order indices");
+    // CUB's kernels are library work: not counted among this library's launches
+    check_cuda(cub::DeviceRadixSort::SortPairsDescending(tmp, temp, (const unsigned int *)counts, keys_out, idx_in,
+                                                        order, (int)n, 0, 32, s),
+               "member order sort");
+}
 
 void order_by_span_f32(const float *tspan, size_t n, int *order, void *scratch, size_t *scratch_bytes, cudaStream_t s)
 {

@@ -192,6 +192,7 @@ struct clode_sim {
     DevBuf x0, pars, xf, rng, dt, tf, tspan_dev, odata, F, t, x, dx, aux, nstored, status, stats, stage, work;
     DevBuf ev_t, ev_x, ev_dx, ev_aux, nevents;  // features with storage: event states
     DevBuf order, order_scratch;                // persistent kernels: members by decreasing time span
+    DevBuf work_counts, order_work;             // warm-up steps per member; the feature pass's order by them
 
     // program
     bool built = false;
@@ -239,6 +240,10 @@ struct clode_sim {
     bool collect_stats = true;
     bool order_by_span = true;  // persistent kernels take the longest per-member time spans first
     bool order_valid = false;   // `order` holds the permutation of the current per-member spans
+    bool order_by_work = true;  // the feature pass of a two-pass observer takes the members with the
+                                // most warm-up steps first (the separate warm-up launch counts them)
+    bool record_work = false;   // the next warm-up launch writes work_counts
+    bool use_work_order = false;  // the next features launch runs members in order_work
     long long range_end = -1;  // autotuner trials: run members [0, range_end) only
     int range_stride = 1;      // ... every range_stride-th of them (persistent kernels)
 
@@ -270,7 +275,7 @@ struct clode_sim {
     {
         return {&x0,  &pars,   &xf,    &rng,    &dt,   &tf,    &tspan_dev, &odata, &F,
                 &t,   &x,      &dx,    &aux,    &nstored, &status, &stats, &stage, &work,
-                &ev_t, &ev_x, &ev_dx, &ev_aux, &nevents, &order, &order_scratch};
+                &ev_t, &ev_x, &ev_dx, &ev_aux, &nevents, &order, &order_scratch, &work_counts, &order_work};
     }
 
     size_t real_size() const { return single ? sizeof(float) : sizeof(double); }
@@ -705,6 +710,7 @@ struct clode_sim {
         a.dx_out = dx.as<R>();
         a.aux_out = aux.as<R>();
         a.n_stored = nstored.as<int>();
+        a.work_out = record_work ? work_counts.as<int>() : nullptr;
         a.ev_t = ev_t.as<R>();
         a.ev_x = ev_x.as<R>();
         a.ev_dx = ev_dx.as<R>();
@@ -764,6 +770,22 @@ struct clode_sim {
         return order.as<int>();
     }
 
+    // The feature pass of a two-pass observer integrates exactly the steps
+    // its warm-up pass took, which counted them per member: sorting by those
+    // counts gives that launch the longest-first order from the work itself
+    // (a member held back by a tiny step size starts first instead of last).
+    // Enqueued inside the features launch's timing; each member's arithmetic
+    // is unchanged.
+    const int *work_order()
+    {
+        size_t scratch = 0;
+        order_by_count(work_counts.as<int>(), (size_t)nPts, nullptr, nullptr, &scratch, stream);
+        order_work.reserve((size_t)nPts * sizeof(int));
+        order_scratch.reserve(scratch);
+        order_by_count(work_counts.as<int>(), (size_t)nPts, order_work.as<int>(), order_scratch.p, &scratch, stream);
+        return order_work.as<int>();
+    }
+
     // grid schedule: one thread per member.  persistent schedule: as many
     // resident blocks as the SMs hold (or blocks_per_sm per SM), lanes pull
     // members from a counter; never more threads than members.
@@ -803,7 +825,7 @@ struct clode_sim {
         }
         last_grid = (int)grid;
         last_block = (int)block;
-        const int *ord = k == kpersist ? member_order() : nullptr;
+        const int *ord = k != kpersist ? nullptr : use_work_order ? work_order() : member_order();
         if (single) {
             ArgsT<float> a = make_args<float>();
             a.fused_init = fused_init;
@@ -907,17 +929,35 @@ struct clode_sim {
         int fused = 0;
         double init_ms = 0.0;
         unsigned long long init_stats[CLODE_STAT_COUNT] = {0};
+        bool by_work = false;
         if (!observer_initialized) {
             if (fuse_init) {
                 fused = 1;
             } else {
-                initialize_observer();
+                by_work = schedule == 1 && order_by_work && obs_two_pass() && nPts > 1 && kp_init != nullptr;
+                if (by_work)
+                    work_counts.reserve((size_t)nPts * sizeof(int));
+                record_work = by_work;
+                try {
+                    initialize_observer();
+                } catch (...) {
+                    record_work = false;
+                    throw;
+                }
+                record_work = false;
                 init_ms = last_ms;
                 memcpy(init_stats, last_stats, sizeof init_stats);
             }
         }
+        use_work_order = by_work;
         begin_run();
-        launch(k_features, kp_features, fused);
+        try {
+            launch(k_features, kp_features, fused);
+        } catch (...) {
+            use_work_order = false;
+            throw;
+        }
+        use_work_order = false;
         end_run("features");
         // time and counters of the whole call, observer initialisation included
         last_ms += init_ms;
@@ -950,17 +990,35 @@ struct clode_sim {
         int fused = 0;
         double init_ms = 0.0;
         unsigned long long init_stats[CLODE_STAT_COUNT] = {0};
+        bool by_work = false;
         if (!observer_initialized) {
             if (fuse_init) {
                 fused = 1;
             } else {
-                initialize_observer();
+                by_work = schedule == 1 && order_by_work && obs_two_pass() && nPts > 1 && kp_init != nullptr;
+                if (by_work)
+                    work_counts.reserve((size_t)nPts * sizeof(int));
+                record_work = by_work;
+                try {
+                    initialize_observer();
+                } catch (...) {
+                    record_work = false;
+                    throw;
+                }
+                record_work = false;
                 init_ms = last_ms;
                 memcpy(init_stats, last_stats, sizeof init_stats);
             }
         }
+        use_work_order = by_work;
         begin_run();
-        launch(k_features, kp_features, fused);
+        try {
+            launch(k_features, kp_features, fused);
+        } catch (...) {
+            use_work_order = false;
+            throw;
+        }
+        use_work_order = false;
         end_run("features with storage");
         last_ms += init_ms;
         for (int k = 0; k < CLODE_STAT_COUNT; ++k)
@@ -1974,6 +2032,8 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
             sim->collect_stats = value != 0.0;
         } else if (k == "order_by_span") {
             sim->order_by_span = value != 0.0;
+        } else if (k == "order_by_work") {
+            sim->order_by_work = value != 0.0;
         } else {
             fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);
         }
@@ -2001,6 +2061,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "fuse_init") *value = sim->fuse_init;
         else if (k == "collect_stats") *value = sim->collect_stats;
         else if (k == "order_by_span") *value = sim->order_by_span;
+        else if (k == "order_by_work") *value = sim->order_by_work;
         else if (k == "last_grid") *value = sim->last_grid;
         else if (k == "last_block") *value = sim->last_block;
         else fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);

@@ -300,7 +300,9 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * launch instead of a launch of its own before it; results are identical),
  * "collect_stats" (0/1), "order_by_span" (0/1, default 1: with per-member time
  * spans the persistent lanes take the members in decreasing order of span;
- * results are the same either way).  Read-only for get_option: "last_grid", "last_block".
+ * results are the same either way), "order_by_work" (0/1, default 1: the
+ * feature pass of a two-pass observer takes the members in decreasing order
+ * of the steps its separate warm-up launch counted; same results).  Read-only for get_option: "last_grid", "last_block".
  * Changing a build option (fmad, prec_div, ftz, fast_math, fast_exp, maxrregcount,
  * split_attempts, step_block) recompiles the program at the next run. */
 int clode_sim_set_option(clode_sim *sim, const char *key, double value);

@@ -276,8 +276,9 @@ def test_stochastic_bitwise_rng_state(single, schedule):
 @pytest.mark.parametrize("fuse", [0, 1])
 def test_longest_span_first_order_changes_nothing(fuse):
     # the persistent lanes take members in decreasing order of their time
-    # span by default; every member's results must equal those of the
-    # natural order bit for bit
+    # span, and the feature pass in decreasing order of the warm-up steps,
+    # by default; every member's results must equal those of the natural
+    # order bit for bit
     n = 3000
     rng = np.random.default_rng(8)
     pars = np.stack([rng.uniform(0.5, 3.0, n), np.full(n, 3.0), rng.uniform(0.0, 2.0, n)], axis=1)
@@ -285,11 +286,14 @@ def test_longest_span_first_order_changes_nothing(fuse):
     tspan = np.stack([np.zeros(n), rng.uniform(200.0, 2000.0, n)], axis=1)
     sc = Scenario("lactotroph.cl", 4, 3, x0, pars, n_aux=1, stepper="dopri5", single=True,
                   observer="nhood2", op=dict(e_var_ix=3, f_var_ix=0), tspan_pm=tspan, steps=[("features", None, True)])
-    runs = [run_engine(sc, options={"schedule": 1, "fuse_init": fuse, "order_by_span": o}) for o in (0, 1)]
-    for k in ("xf", "tf", "dt"):
-        assert np.array_equal(runs[0][k], runs[1][k], equal_nan=True), k
-    assert np.array_equal(runs[0]["F_list"][0], runs[1]["F_list"][0], equal_nan=True)
-    assert runs[0]["stats"] == runs[1]["stats"]
+    # (span order, warm-up-steps order of the feature pass): neither, both, each alone
+    runs = [run_engine(sc, options={"schedule": 1, "fuse_init": fuse, "order_by_span": o, "order_by_work": w})
+            for o, w in ((0, 0), (1, 1), (1, 0), (0, 1))]
+    for r in runs[1:]:
+        for k in ("xf", "tf", "dt"):
+            assert np.array_equal(runs[0][k], r[k], equal_nan=True), k
+        assert np.array_equal(runs[0]["F_list"][0], r["F_list"][0], equal_nan=True)
+        assert runs[0]["stats"] == r["stats"]
 
 
 def test_all_zero_rng_state_is_rejected():
