@@ -168,3 +168,37 @@ def test_log_levels_and_sink(capfd):
     W._log(W.LogLevel.warn, "patterned")
     assert capfd.readouterr().out.strip() == "warning: patterned"
     lg.set_log_pattern("[%Y-%m-%d %H:%M:%S.%e] [%n] [%l] %v")
+
+
+def test_storage_and_order_entry_points_validate_on_the_host():
+    # the additions of the one-pass store, stored subsets, member orders and
+    # member-major fetches check their arguments before touching a device
+    cp, keep = _problem("lactotroph.cl", 4, 3, 1, 0)
+    op = N.CObserverParams(3, 0, 100, 0, 0, 0, 0.05, 0.2, 0.2, 0, 0, 0)
+    h = C.c_void_p()
+    N.check(N.lib.clode_sim_create(N.SIM_FEATURES, C.byref(cp), b"dopri5", b"nhood2", C.byref(op), 1, 0,
+                                   C.byref(h)))
+    try:
+        ix = (C.c_int * 2)(3, 0)
+        bad = (C.c_int * 1)(4)
+        N.check(N.lib.clode_sim_set_store_variables(h, ix, 2, None, 0))
+        assert N.lib.clode_sim_set_store_variables(h, bad, 1, None, -1) == 1
+        assert b"outside" in N.lib.clode_last_error()
+        assert N.lib.clode_sim_set_store_variables(h, None, 1, None, -1) == 1
+        N.check(N.lib.clode_sim_set_store_variables(h, None, -1, None, -1))
+        # nothing stored yet: no rows, no events, fetches refused
+        n = C.c_size_t(7)
+        N.check(N.lib.clode_sim_get_n_events(h, None, 0, C.byref(n)))
+        assert n.value == 0
+        assert N.lib.clode_sim_get_trajectory_by_member(h, 0, 0, 0, None, None, None, None, None) == 1
+        assert N.lib.clode_sim_get_events_by_member(h, 0, 0, 0, None, None, None, None, None) == 1
+        assert N.lib.clode_sim_features_store(h, 1, 4) == 7  # no problem data yet
+        for key in (b"order_by_span", b"order_by_work"):
+            v = C.c_double(-1)
+            N.check(N.lib.clode_sim_get_option(h, key, C.byref(v)))
+            assert v.value == 1.0
+            N.check(N.lib.clode_sim_set_option(h, key, 0.0))
+            N.check(N.lib.clode_sim_get_option(h, key, C.byref(v)))
+            assert v.value == 0.0
+    finally:
+        N.lib.clode_sim_destroy(h)
