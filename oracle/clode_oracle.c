@@ -1228,6 +1228,67 @@ void o_features(int nPts, int i0, int i1, int nthreads, const realtype *tspan, i
         o_member_store(&m, i, nPts, xf, rng, dtv, tf);
     }
 }
+
+/* Features with storage (no reference counterpart: the reference's unified
+ * driver clode/cpp/odedriver.cl:10-162 does not compile): o_features, plus
+ * the trajectory rows of that pass stored as o_trajectory stores them
+ * (trajectory.cl:63-95: row 0, then every nout-th step while row < max_store,
+ * without ending the loop) and the state at each of the first ev_rows
+ * observer events, rows [k][var][member]; n_stored and n_events per member. */
+void o_features_store(int nPts, int i0, int i1, int nthreads, const realtype *tspan, int tspan_stride,
+                      realtype *x0, const realtype *pars, const void *spv, realtype *xf, uint64_t *rng, realtype *dtv,
+                      realtype *tf, void *odata, const void *opv, realtype *F, realtype *tout, realtype *xout,
+                      realtype *dxout, realtype *auxout, int *nStored, int ev_rows, realtype *evt, realtype *evx,
+                      realtype *evdx, realtype *evaux, int *nEvents)
+{
+    const o_solver_params *sp = (const o_solver_params *)spv;
+    const o_observer_params *op = (const o_observer_params *)opv;
+    o_obs *obs = (o_obs *)odata;
+    if (nthreads < 1) nthreads = 1;
+    OMP_MEMBERS
+    for (int i = i0; i < i1; ++i) {
+        const realtype *ts = tspan + (long)tspan_stride * i;
+        o_member m;
+        o_member_load(&m, i, nPts, ts, x0, pars, rng, dtv);
+        o_obs o = obs[i];
+        long row = 0, ev = 0;
+#define O_STORE_STATE(T, X, DX, AUX, R)                                               \
+        do {                                                                          \
+            T[(R) * nPts + i] = m.t;                                                  \
+            for (int j = 0; j < N_VAR; ++j)                                           \
+                X[(R) * nPts * N_VAR + (long)j * nPts + i] = m.x[j];                  \
+            for (int j = 0; j < N_VAR; ++j)                                           \
+                DX[(R) * nPts * N_VAR + (long)j * nPts + i] = m.dx[j];                \
+            for (int j = 0; j < N_AUX; ++j)                                           \
+                AUX[(R) * nPts * N_AUX + (long)j * nPts + i] = m.aux[j];              \
+        } while (0)
+        O_STORE_STATE(tout, xout, dxout, auxout, row);
+        unsigned int step = 0;
+        while (m.t <= ts[1] && step < sp->max_steps) {
+            ++step;
+            o_stepper(&m.t, m.x, m.dx, m.p, sp, &m.dt, ts, m.aux, m.w, &m.r);
+            if (step % sp->nout == 0 && row < (long)sp->max_store) {
+                ++row;
+                O_STORE_STATE(tout, xout, dxout, auxout, row);
+            }
+            ob_update(m.t, m.x, m.dx, m.aux, &o, op);
+            if (ob_event(m.t, m.x, m.dx, m.aux, &o, op)) {
+                if (ev < ev_rows)
+                    O_STORE_STATE(evt, evx, evdx, evaux, ev);
+                ++ev;
+                if (ob_on_event(m.t, m.x, m.dx, m.aux, &o, op))
+                    break;
+            }
+        }
+#undef O_STORE_STATE
+        nStored[i] = (int)row;
+        nEvents[i] = (int)ev;
+        ob_write(&o, F, i, nPts);
+        ob_rebase(m.t - ts[0], &o);
+        obs[i] = o;
+        o_member_store(&m, i, nPts, xf, rng, dtv, tf);
+    }
+}
 #else
 int o_odata_size(void) { return 0; }
 #endif

@@ -76,6 +76,7 @@ class OracleSimulator:
 
     def __init__(self, cfg: OracleConfig, reference: bool = False, nthreads: int | None = None):
         self.cfg = cfg
+        self.reference = reference
         self.path = build_reference(cfg) if reference else build_port(cfg)
         self.lib = C.CDLL(self.path)
         self.real = np.float32 if cfg.single_precision else np.float64
@@ -201,6 +202,35 @@ class OracleSimulator:
                               _ptr(self.pars), C.byref(self.sp), _ptr(self.xf), _ptr(self.rng), _ptr(self.dt),
                               _ptr(self.tf), _ptr(self.t), _ptr(self.x), _ptr(self.dx), _ptr(self.aux),
                               _ptr(self.n_stored))
+
+    def features_store(self, event_rows: int, reinitialize: bool | None = None):
+        """features() that also stores the trajectory rows and the first
+        event_rows event states (o_features_store, the port only)."""
+        if self.reference:
+            raise RuntimeError("features with storage exist in the port only")
+        if reinitialize is not None:
+            self.observer_initialized = not reinitialize
+        self._resize_features()
+        if not self.observer_initialized:
+            self.initialize_observer()
+        ms = int(self.sp.max_store)
+        n, nv, na = self.nPts, self.cfg.n_var, self.cfg.n_aux
+        self.t = np.zeros((ms + 1) * n, dtype=self.real)
+        self.x = np.zeros((ms + 1) * n * nv, dtype=self.real)
+        self.dx = np.zeros((ms + 1) * n * nv, dtype=self.real)
+        self.aux = np.zeros(max((ms + 1) * n * na, 1), dtype=self.real)
+        self.n_stored = np.zeros(n, dtype=np.int32)
+        self.ev_t = np.zeros(max(event_rows * n, 1), dtype=self.real)
+        self.ev_x = np.zeros(max(event_rows * n * nv, 1), dtype=self.real)
+        self.ev_dx = np.zeros(max(event_rows * n * nv, 1), dtype=self.real)
+        self.ev_aux = np.zeros(max(event_rows * n * na, 1), dtype=self.real)
+        self.n_events = np.zeros(n, dtype=np.int32)
+        self.lib.o_features_store(n, 0, n, self.nthreads, _ptr(self.tspan), self.tspan_stride, _ptr(self.x0),
+                                  _ptr(self.pars), C.byref(self.sp), _ptr(self.xf), _ptr(self.rng), _ptr(self.dt),
+                                  _ptr(self.tf), _ptr(self.odata), C.byref(self.op), _ptr(self.F), _ptr(self.t),
+                                  _ptr(self.x), _ptr(self.dx), _ptr(self.aux), _ptr(self.n_stored), int(event_rows),
+                                  _ptr(self.ev_t), _ptr(self.ev_x), _ptr(self.ev_dx), _ptr(self.ev_aux),
+                                  _ptr(self.n_events))
 
     # ----------------------------------------------------------- getters --
     def get_xf(self) -> np.ndarray:

@@ -241,3 +241,40 @@ def test_events_by_member_match_the_flat_arrays():
     part = store.get_events_by_member(first=100, count=20, rows=ev_rows)
     assert part["t"].shape == (20, ev_rows)
     assert _same(part["t"], regroup_by_member(store.get_event_t(), N, 1, 100, 20, ev_rows)[:, :, 0])
+
+
+def test_store_run_equals_the_oracle_bitwise():
+    # Lorenz (+ - * only), RK4 in FP64, thresh2: the engine's one-pass store
+    # against the oracle's restatement of it, bit for bit
+    from oracle.build import OracleConfig
+    from oracle.runner import OracleSimulator
+    n = 300
+    rng = np.random.default_rng(4)
+    x0 = np.ones((n, 3)) + rng.normal(0, 1e-3, (n, 3))
+    pars = np.stack([rng.uniform(10, 60, n), rng.uniform(5, 15, n), np.full(n, 8 / 3)], axis=1)
+    sp = dict(dt=1e-3, max_steps=100000, max_store=3000, nout=5)
+    opk = dict(e_var_ix=2, f_var_ix=2, max_event_count=100000, x_up_threshold=0.3, x_down_threshold=0.2)
+    pi = W.ProblemInfo(rhs_path("lorenz.cl"), ["x", "y", "z"], ["rho", "sigma", "beta"], ["fx"], 0)
+    sim = W.FeatureSimulatorBase(pi, "rk4", "thresh2", W.ObserverParams(**opk), False, W.OpenCLResource(), "")
+    sim.set_option("schedule", 1)
+    sim.set_solver_params(W.SolverParams(dtmax=1.0, abstol=1e-6, reltol=1e-3, **sp))
+    sim.set_problem_data(x0.flatten(order="F"), pars.flatten(order="F"))
+    sim.set_tspan([0.0, 10.0])
+    sim.features_store(True, event_rows=8)
+    cfg = OracleConfig(rhs_path("lorenz.cl"), n_var=3, n_par=3, n_aux=1, stepper="rk4", single_precision=False,
+                       observer="thresh2", n_store_events=0)
+    ora = OracleSimulator(cfg)
+    ora.set_solver_params(**sp)
+    ora.set_observer_params(**opk)
+    ora.set_problem_data(x0, pars)
+    ora.set_tspan((0.0, 10.0))
+    ora.features_store(event_rows=8, reinitialize=True)
+    ms = 3000
+    assert np.array_equal(sim.get_f(), ora.F.astype(np.float64))
+    assert np.array_equal(sim.get_n_stored(), ora.n_stored)
+    assert np.array_equal(sim.get_t(), ora.t[: ms * n])
+    assert np.array_equal(sim.get_x(), ora.x[: ms * n * 3])
+    assert np.array_equal(sim.get_dx(), ora.dx[: ms * n * 3])
+    assert np.array_equal(sim.get_n_events(), ora.n_events)
+    for k in ("t", "x", "dx", "aux"):
+        assert np.array_equal(getattr(sim, "get_event_" + k)(), getattr(ora, "ev_" + k)), k
