@@ -14,10 +14,15 @@
 //                A two-pass observer's warm-up pass runs as its own launch
 //                (clode_init_observer_persistent) or, fused, inside the
 //                features launch through the same stepper call as the
-//                feature pass.
+//                feature pass.  The host may hand out the members through a
+//                permutation (`order`: longest time spans first, or the
+//                feature pass by the warm-up's step counts).
+//
+// Programs built with CLODE_FEATURE_STORE also store, in the feature pass,
+// the trajectory rows and the state at observer events (FeatureStore).
 //
 // Per member, both schedules execute the same arithmetic in the same order,
-// so their results are identical.  Member semantics follow
+// so their results are identical whatever order the members are taken in.  Member semantics follow
 // clode/cpp/transient.cl:9-77, initializeObserver.cl:9-84, features.cl:10-106
 // and trajectory.cl:14-112.
 #pragma once
