@@ -202,3 +202,20 @@ def test_storage_and_order_entry_points_validate_on_the_host():
             assert v.value == 0.0
     finally:
         N.lib.clode_sim_destroy(h)
+
+
+@pytest.mark.parametrize("single", [True, False], ids=["fp32", "fp64"])
+def test_xpp_style_model_with_float_literals_builds(single):
+    # decimal literals with an `f` suffix (what clODE's XPP translator emits)
+    # compile in both precisions, as in OpenCL C
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models", "xpp_style.cl")
+    src = open(path, "rb").read()
+    cp = N.CProblem(src, b"xpp_style.cl", 2, 2, 1, 0, b"v\nr", b"a\nb", b"drive")
+    op = N.CObserverParams(0, 0, 100, 0, 0, 0, 0.05, 0.2, 0.2, 0, 0, 0)
+    h = C.c_void_p()
+    N.check(N.lib.clode_sim_create(N.SIM_FEATURES, C.byref(cp), b"rk4", b"localmax", C.byref(op), int(single), 0,
+                                   C.byref(h)))
+    try:
+        N.check(N.lib.clode_sim_build(h))
+    finally:
+        N.lib.clode_sim_destroy(h)

@@ -334,3 +334,20 @@ def test_time_budget_marks_unprocessed_members():
     assert (status[~done] == 16).all()
     ora = run_oracle(sc)
     np.testing.assert_array_equal(eng["xf"][done], ora["xf"][done])
+
+
+def test_xpp_style_float_literals_match_the_oracle():
+    # literals with an `f` suffix (clODE's XPP translator) are float constants
+    # promoted in FP64 arithmetic on both sides, so the FP64 RK4 run matches
+    # the oracle bit for bit in the state (the aux feature uses exp: 1e-12)
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models", "xpp_style.cl")
+    n = 512
+    rng = np.random.default_rng(21)
+    x0 = rng.uniform(-2.0, 2.0, (n, 2))
+    pars = np.stack([rng.uniform(0.5, 0.9, n), rng.uniform(0.6, 0.9, n)], axis=1)
+    sc = Scenario(path, 2, 2, x0, pars, n_aux=1, stepper="rk4", observer="localmax", single=False,
+                  sp=dict(dt=0.01, max_steps=1000000), steps=[("features", (0.0, 60.0), True)])
+    eng, ora = run_engine(sc), run_oracle(sc)
+    assert_bitwise(eng, ora, keys=("xf", "tf", "dt"))
+    np.testing.assert_allclose(eng["F_list"][0], ora["F_list"][0], rtol=1e-12, atol=1e-14)
