@@ -9,7 +9,8 @@ configuration (precision, stepper, observer, sizes, model source):
   (clode/cpp/{transient,initializeObserver,features,trajectory}.cl), compiled
   in place as C11 through ``ref_shim.h``/``ref_driver.c`` into
   ``oracle/_ref/``.  Only possible where the clODE source tree is present
-  (``CLODE_REFERENCE_ROOT``, default ``/root/reference``).
+  (``CLODE_REFERENCE_ROOT``; without it, a clODE checkout named
+  ``reference`` beside this repository's root directory).
 
 Both are compiled with ``-ffp-contract=off`` so that no multiply-add is fused
 behind the reference's back, and with OpenMP over members when the compiler
@@ -28,7 +29,8 @@ from dataclasses import dataclass, field
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("CLODE_REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get("CLODE_REFERENCE_ROOT",
+                                os.path.normpath(os.path.join(HERE, os.pardir, os.pardir, "reference")))
 REFERENCE_KERNEL_DIR = os.path.join(REFERENCE_ROOT, "clode", "cpp")
 
 # stepper name -> define, clode/cpp/steppers.cl:26-43

@@ -2,7 +2,8 @@
 
 Runs every scenario of ``scenarios.py`` through clODE's own kernel sources
 compiled as C (``oracle/build.py build_reference``; needs the clODE source
-tree, default /root/reference, override with CLODE_REFERENCE_ROOT) and saves
+tree: CLODE_REFERENCE_ROOT, else a checkout named ``reference`` beside the
+repository) and saves
 inputs and outputs as ``<name>.npz``.  Usage: ``python -m tests.golden.make_golden``.
 """
 import json
