@@ -71,6 +71,7 @@ struct NoallocFeaturesLaunch {
     void *kernel;          // cudaKernel_t of clode_features_persistent
     int single;            // working precision is float
     unsigned int obs_words;
+    int n_par;             // parameter columns the kernel reads from pars
     int device;
     int block;
     unsigned char args[512];  // ArgsT<float> or ArgsT<double>

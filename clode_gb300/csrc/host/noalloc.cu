@@ -1,17 +1,17 @@
 // clode_sim_features_noalloc: a features run for callers that cannot
 // allocate device memory.
 //
-// Some callers are not allowed to call cudaMalloc at run time: code that
-// runs while a CUDA graph is being captured (an allocation there breaks the
-// capture), services whose device memory is carved up once at start-up and
-// whose allocator refuses later requests, and real-time pipelines that
-// forbid allocation after initialisation because it can block on the
-// driver.  The regular features() path allocates its feature, state and
-// scratch buffers on the device the first time it sees an ensemble size.
-// This entry point takes every input and output buffer from the caller and
-// keeps its own scratch — the member work counter of the persistent schedule
-// and the observer state parked at the end of each member — in one
-// file-scope device array, so it calls no allocating routine at all.
+// Some callers are not allowed to call cudaMalloc at run time: services
+// whose device memory is carved up once at start-up and whose allocator
+// refuses later requests, real-time pipelines that forbid allocation after
+// initialisation because it can block on the driver, and plug-ins hosted by
+// an application that owns every device allocation itself.  The regular
+// features() path allocates its feature, state and scratch buffers on the
+// device the first time it sees an ensemble size.  This entry point takes
+// every input and output buffer from the caller and keeps its own scratch —
+// the member work counter of the persistent schedule and the observer state
+// parked at the end of each member — in one file-scope device array, so it
+// calls no allocating routine at all.
 //
 // The array (kScratchBytes, 64 MiB) is created by the CUDA runtime when this
 // library's device code is loaded on a GPU and stays there until the process
@@ -38,7 +38,10 @@ std::mutex g_mu;
 void *g_scratch_addr[kMaxDevices] = {nullptr};
 
 // Device address of g_scratch on `device`, which must be current; looked up
-// once per device and remembered.
+// once per device and remembered.  The remembered address belongs to the
+// device's primary context (the one the CUDA runtime uses): it stays valid
+// for the life of the process unless that context is destroyed
+// (cudaDeviceReset), after which this entry point must not be called.
 void *scratch_address(int device)
 {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -81,6 +84,24 @@ void launch_features(A &a, const clode::NoallocFeaturesLaunch &L, long long n_pt
     clode::count_launch();
 }
 
+// Makes `device` current for the lifetime of the guard and gives the
+// calling thread its previous current device back on every exit path.
+struct CurrentDevice {
+    int saved = -1;
+    explicit CurrentDevice(int device)
+    {
+        clode::check_cuda(cudaGetDevice(&saved), "cudaGetDevice");
+        if (saved != device)
+            clode::check_cuda(cudaSetDevice(device), "cudaSetDevice");
+    }
+    ~CurrentDevice()
+    {
+        int now = -1;
+        if (saved >= 0 && cudaGetDevice(&now) == cudaSuccess && now != saved)
+            cudaSetDevice(saved);
+    }
+};
+
 }  // namespace
 
 extern "C" int clode_sim_features_noalloc(clode_sim *sim, long long n_pts, const void *x0, const void *pars,
@@ -105,7 +126,10 @@ extern "C" int clode_sim_features_noalloc(clode_sim *sim, long long n_pts, const
                         n_pts, need, per_member, kScratchBytes, (kScratchBytes - kHeaderBytes) / per_member);
         if (!x0 || !rng || !dt || !xf || !tf || !F)
             clode::fail(CLODE_ERR_INVALID_ARGUMENT, "x0, rng, dt, xf, tf and F must be device pointers");
-        clode::check_cuda(cudaSetDevice(L.device), "cudaSetDevice");
+        if (L.n_par > 0 && !pars)
+            clode::fail(CLODE_ERR_INVALID_ARGUMENT, "pars must be a device pointer: the model has %d parameters",
+                        L.n_par);
+        CurrentDevice on_device(L.device);
         unsigned char *base = (unsigned char *)scratch_address(L.device);
         cudaStream_t s = (cudaStream_t)stream;
         // the work counter must start at zero; the parked observer state of a

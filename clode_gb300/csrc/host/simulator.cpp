@@ -2118,6 +2118,7 @@ void noalloc_features_prepare(clode_sim *sim, NoallocFeaturesLaunch *out)
     out->kernel = (void *)sim->kp_features;
     out->single = sim->single ? 1 : 0;
     out->obs_words = sim->obs_words;
+    out->n_par = sim->nPar;
     out->device = sim->lib_device;
     out->block = std::max(32, std::min(1024, sim->block_size));
     if (sim->single) {

@@ -329,29 +329,34 @@ int clode_sim_autotune(clode_sim *sim, long long sample, double *best_ms);
 unsigned long long clode_launch_count(void);
 /* features() for callers that cannot allocate device memory.  No counterpart
  * in the reference.  Some callers may not call cudaMalloc once they are
- * running: code inside a CUDA graph capture (an allocation breaks the
- * capture), services whose device memory is partitioned once at start-up,
- * real-time pipelines that forbid allocation after initialisation.  The
- * regular path allocates its buffers on first use; this one allocates
- * nothing.  The caller passes every input and output as a device pointer in
- * the simulator's working precision (float if single precision, else
- * double), SoA [j*n_pts + i]: x0 and pars (nVar and nPar columns), tspan
- * (per member [2i], [2i+1]; NULL = the simulator's tspan), rng (2*n_pts
- * words) and dt (n_pts), read and updated in place, xf (nVar columns), tf,
- * F (nFeatures columns) and optionally status (NULL = not written).  The
- * observer is initialised inside the launch on every call.
+ * running: services whose device memory is partitioned once at start-up,
+ * real-time pipelines that forbid allocation after initialisation (it can
+ * block on the driver), plug-ins whose host application owns every device
+ * allocation.  The regular path allocates its buffers on first use; this one
+ * allocates nothing.  The caller passes every input and output as a device
+ * pointer in the simulator's working precision (float if single precision,
+ * else double), SoA [j*n_pts + i]: x0 and pars (nVar and nPar columns; pars
+ * may be NULL only when nPar is 0), tspan (per member [2i], [2i+1]; NULL =
+ * the simulator's tspan), rng (2*n_pts words) and dt (n_pts), read and
+ * updated in place, xf (nVar columns), tf, F (nFeatures columns) and
+ * optionally status (NULL = not written).  The observer is initialised
+ * inside the launch on every call.
  * Scratch (the work counter and the observer state parked per member) lives
  * in one fixed 64 MiB device array compiled into the library: held on every
  * GPU that loads the library until the process exits; n_pts beyond what it
  * holds for the observer (64 MiB / state bytes per member) is rejected with
- * CLODE_ERR_INVALID_ARGUMENT.  The array's device address is looked up on the
- * first call on each device, so make that first call before any stream
- * capture.  The launch is enqueued on `stream` (a cudaStream_t; NULL = the
+ * CLODE_ERR_INVALID_ARGUMENT.  The first call on each device looks up the
+ * array's device address (in that device's primary context, which must not
+ * be reset with cudaDeviceReset afterwards), so make that first call before
+ * any stream capture.  The call makes the simulator's device current while it
+ * runs and restores the caller's current device before it returns.  The
+ * launch is enqueued on `stream` (a cudaStream_t of that device; NULL = the
  * default stream) and the call returns without waiting; every call shares the
- * one array, so calls that overlap on the GPU race and must be ordered by the
- * caller.  The simulator must be a feature simulator built on its device
- * (clode_sim_build) after its last observer-parameter change and after its
- * last clode_sim_features_store (which loads a program that stores rows). */
+ * one array and keeps the last call's contents, so calls that overlap on the
+ * GPU race and must be ordered by the caller.  The simulator must be a
+ * feature simulator built on its device (clode_sim_build) after its last
+ * observer-parameter change and after its last clode_sim_features_store
+ * (which loads a program that stores rows). */
 int clode_sim_features_noalloc(clode_sim *sim, long long n_pts, const void *x0, const void *pars,
                                const void *tspan, unsigned long long *rng, void *dt, void *xf, void *tf,
                                void *F, int *status, void *stream);
