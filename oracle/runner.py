@@ -109,7 +109,12 @@ class OracleSimulator:
         op.dxUpThresh, op.dxDownThresh, op.eps_dx = dx_up_threshold, dx_down_threshold, eps_dx
 
     def set_tspan(self, tspan):
+        """One [t0, t1] for every member, or a pair per member: shaped
+        (nPts, 2), or flat [t0_0, t1_0, t0_1, t1_1, ...] as the engine's
+        set_tspan_per_member takes it."""
         ts = np.asarray(tspan, dtype=np.float64)
+        if ts.ndim == 1 and ts.size > 2:
+            ts = ts.reshape(-1, 2)
         if ts.ndim == 1:
             self.tspan = np.ascontiguousarray(ts[:2].astype(self.real))
             self.tspan_stride = 0
