@@ -53,7 +53,7 @@ OBSERVER_DEFINES = {
     "thresh2": "USE_OBSERVER_THRESHOLD_2",
 }
 
-CFLAGS = ["-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-w"]
+CFLAGS = ["-O3", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-w"]
 
 
 @dataclass(frozen=True)
