@@ -523,6 +523,10 @@ def main():
     ap.add_argument("--split-attempts", type=int, default=None)
     ap.add_argument("--fuse-init", type=int, default=None)
     ap.add_argument("--step-block", type=int, default=None)
+    ap.add_argument("--replay", type=int, default=None,
+                    help="feature pass replays the warm-up's stored steps (engine default 1)")
+    ap.add_argument("--replay-mb", type=float, default=None, help="record regions in MiB (engine default: automatic)")
+    ap.add_argument("--precise", type=int, default=None, help="the engine's precision option (engine default 0)")
     ap.add_argument("--autotune", type=int, default=1048576,
                     help="autotune on a strided sample of this many members first (0: off)")
     ap.add_argument("--surrogate-grid", type=int, default=4096)
@@ -580,7 +584,8 @@ def main():
                      ("fast_exp", args.fast_exp), ("split_attempts", args.split_attempts),
                      ("fuse_init", args.fuse_init), ("step_block", args.step_block),
                      ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm),
-                     ("order_by_span", args.order_by_span)):
+                     ("order_by_span", args.order_by_span), ("replay", args.replay), ("replay_mb", args.replay_mb),
+                     ("precise", args.precise)):
         if val is not None:
             sim.set_option(key, val)
     sim.build_cl()

@@ -103,6 +103,25 @@ struct ArgsT {
     const int *order;
     // persistent observer initialisation: each member's warm-up steps (null: not recorded)
     int *work_out;
+    // replay of the warm-up pass (two-pass observers): the recording warm-up
+    // launch stores every step of the feature pass in per-warp regions of
+    // rec_rows rows, [((warp * rec_rows + row) * fields + field) * 32 + lane];
+    // per row the lanes with a step and the lanes whose member starts there,
+    // rec_mask[2 * (warp * rec_rows + row) + {0, 1}]; the members in the
+    // order they start, rec_member[warp * rec_members + k]; rows recorded,
+    // rec_used[warp]; the state at the end of each member's feature pass,
+    // fin[i * stride + word]; and the members the replay cannot finish
+    // (fallback[0 .. *fallback_count)), which the plain feature pass runs.
+    R *rec;
+    unsigned int *rec_mask;
+    int *rec_member;
+    unsigned int *rec_used;
+    unsigned long long rec_rows;
+    unsigned long long rec_fetch_rows;  // a warp takes no new member once this many rows are recorded
+    unsigned int rec_members;
+    unsigned int *fin;
+    int *fallback;
+    unsigned int *fallback_count;
     SolverParamsT<R> sp;
     ObserverParamsT<R> op;
 };

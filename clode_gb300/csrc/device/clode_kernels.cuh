@@ -31,6 +31,14 @@
 #define CLODE_FEATURE_STORE 0
 #endif
 
+// Register cap of the ensemble kernels (the host's maxrregcount option), set
+// per kernel so that the replay kernel can keep its own.
+#if defined(CLODE_MAXNREG) && CLODE_MAXNREG > 0
+#define CLODE_CAP __maxnreg__(CLODE_MAXNREG)
+#else
+#define CLODE_CAP
+#endif
+
 namespace clode {
 
 typedef ArgsT<realtype> Args;
@@ -65,6 +73,7 @@ __device__ __forceinline__ void member_load(Member &m, const Args &a, int i, Cou
 {
     const unsigned long long n = (unsigned long long)a.nPts;
     m.t = member_t0(a, i);
+    m.tlo = ZERO;
     m.dt = a.dt[i];
 #pragma unroll
     for (int j = 0; j < N_PAR; ++j)
@@ -107,19 +116,25 @@ __device__ __forceinline__ void member_store(const Member &m, const Args &a, int
     a.tf[i] = m.t;
 }
 
-__device__ __forceinline__ int member_status_bits(const Member &m, unsigned int step, const Args &a,
-                                                  realtype t1, bool hmin_fail, bool terminal)
+__device__ __forceinline__ int status_bits(realtype t, const realtype (&x)[N_VAR], unsigned int step, const Args &a,
+                                           realtype t1, bool hmin_fail, bool terminal)
 {
     int s = 0;
     if (hmin_fail) s |= STATUS_HMIN_FAIL;
     if (terminal) s |= STATUS_TERMINAL_EVENT;
-    bool finite = isfinite(m.t);
+    bool finite = isfinite(t);
 #pragma unroll
     for (int j = 0; j < N_VAR; ++j)
-        finite = finite && isfinite(m.x[j]);
+        finite = finite && isfinite(x[j]);
     if (!finite) s |= STATUS_NONFINITE;
-    if (!terminal && step >= a.sp.max_steps && m.t <= t1) s |= STATUS_MAX_STEPS;
+    if (!terminal && step >= a.sp.max_steps && t <= t1) s |= STATUS_MAX_STEPS;
     return s;
+}
+
+__device__ __forceinline__ int member_status_bits(const Member &m, unsigned int step, const Args &a,
+                                                  realtype t1, bool hmin_fail, bool terminal)
+{
+    return status_bits(m.t, m.x, step, a, t1, hmin_fail, terminal);
 }
 
 // Sum per-thread counters over the warp and add them to the launch totals.
@@ -191,7 +206,7 @@ __device__ __forceinline__ void run_transient(const Args &a, int i, Counters &c)
     const realtype t1 = member_t1(a, i);
     unsigned int step = 0;
     bool hmin_fail = false;
-    while (m.t <= t1 && step < a.sp.max_steps) {
+    while (t_le(m, t1) && step < a.sp.max_steps) {
         ++step;
         hmin_fail |= step_member(m, a.sp, t1, c) != 0;
     }
@@ -200,7 +215,7 @@ __device__ __forceinline__ void run_transient(const Args &a, int i, Counters &c)
         a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, false);
 }
 
-extern "C" __global__ void clode_transient(const Args a)
+extern "C" __global__ void CLODE_CAP clode_transient(const Args a)
 {
     Counters c = {0, 0, 0, 0};
     int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
@@ -210,7 +225,7 @@ extern "C" __global__ void clode_transient(const Args a)
 }
 
 // transient, persistent schedule: each lane refills itself as its member ends
-extern "C" __global__ void clode_transient_persistent(const Args a)
+extern "C" __global__ void CLODE_CAP clode_transient_persistent(const Args a)
 {
     Counters c = {0, 0, 0, 0};
     const unsigned long long t_start = globaltimer_ns();
@@ -246,7 +261,7 @@ extern "C" __global__ void clode_transient_persistent(const Args a)
             continue;
         bool running = true;
         for (int k = 0; k < CLODE_STEP_BLOCK; ++k) {
-            running = sc.retry || (m.t <= t1 && step < a.sp.max_steps);
+            running = sc.retry || (t_le(m, t1) && step < a.sp.max_steps);
             if (!running)
                 break;
             if (!sc.retry)
@@ -315,7 +330,7 @@ __device__ __forceinline__ void run_trajectory(const Args &a, int i, Counters &c
     unsigned int step = 0;
     unsigned int to_store = a.sp.nout;  // steps until the next stored row (step % nout == 0)
     bool hmin_fail = false;
-    while (m.t <= t1 && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store) {
+    while (t_le(m, t1) && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store) {
         ++step;
         hmin_fail |= step_member(m, a.sp, t1, c) != 0;
         if (--to_store == 0) {
@@ -330,7 +345,7 @@ __device__ __forceinline__ void run_trajectory(const Args &a, int i, Counters &c
         a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, false);
 }
 
-extern "C" __global__ void clode_trajectory(const Args a)
+extern "C" __global__ void CLODE_CAP clode_trajectory(const Args a)
 {
     Counters c = {0, 0, 0, 0};
     int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
@@ -340,7 +355,7 @@ extern "C" __global__ void clode_trajectory(const Args a)
 }
 
 // trajectory, persistent schedule
-extern "C" __global__ void clode_trajectory_persistent(const Args a)
+extern "C" __global__ void CLODE_CAP clode_trajectory_persistent(const Args a)
 {
     Counters c = {0, 0, 0, 0};
     const unsigned long long t_start = globaltimer_ns();
@@ -381,7 +396,7 @@ extern "C" __global__ void clode_trajectory_persistent(const Args a)
             continue;
         bool running = true;
         for (int k = 0; k < CLODE_STEP_BLOCK; ++k) {
-            running = sc.retry || (m.t <= t1 && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store);
+            running = sc.retry || (t_le(m, t1) && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store);
             if (!running)
                 break;
             if (!sc.retry)
@@ -450,13 +465,14 @@ __device__ __forceinline__ void init_observer_member(Observer &o, const Args &a,
     if (Observer::two_pass) {
         const realtype t1 = member_t1(a, i);
         unsigned int step = 0;
-        while (m.t < t1 && step < a.sp.max_steps) {
+        while (t_lt(m, t1) && step < a.sp.max_steps) {
             ++step;
             step_member(m, a.sp, t1, c);
             o.warmup(m.t, m.x, m.dx, m.aux, a.op);
         }
         // rewind to the initial state (the last noise sample is kept)
         m.t = member_t0(a, i);
+        m.tlo = ZERO;
         load_x0(m.x, a, i);
         getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
         c.rhs += 1;
@@ -464,7 +480,7 @@ __device__ __forceinline__ void init_observer_member(Observer &o, const Args &a,
     o.arm(m.t, m.x, m.dx, m.aux, a.op);
 }
 
-extern "C" __global__ void clode_init_observer(const Args a)
+extern "C" __global__ void CLODE_CAP clode_init_observer(const Args a)
 {
     Counters c = {0, 0, 0, 0};
     int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
@@ -480,7 +496,7 @@ extern "C" __global__ void clode_init_observer(const Args a)
 // every lane runs the same (warm-up) pass, so the observer code never
 // diverges between passes.  Not subject to the time budget: every member's
 // observer is initialised.
-extern "C" __global__ void clode_init_observer_persistent(const Args a)
+extern "C" __global__ void CLODE_CAP clode_init_observer_persistent(const Args a)
 {
     Counters c = {0, 0, 0, 0};
     bool exhausted = false;
@@ -516,7 +532,7 @@ extern "C" __global__ void clode_init_observer_persistent(const Args a)
         }
         bool running = Observer::two_pass;
         for (int k = 0; k < CLODE_STEP_BLOCK && running; ++k) {
-            running = sc.retry || (step < a.sp.max_steps && m.t < t1);
+            running = sc.retry || (step < a.sp.max_steps && t_lt(m, t1));
             if (!running)
                 break;
             if (!sc.retry)
@@ -528,6 +544,7 @@ extern "C" __global__ void clode_init_observer_persistent(const Args a)
             if (Observer::two_pass) {
                 // rewind to the initial state (the last noise sample is kept)
                 m.t = member_t0(a, i);
+                m.tlo = ZERO;
                 load_x0(m.x, a, i);
                 getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
                 c.rhs += 1;
@@ -606,7 +623,7 @@ __device__ __forceinline__ void features_member(Observer &o, const Args &a, int 
     FeatureStore fs;
     fs.start(a, m, i);
 #endif
-    while (m.t <= t1 && step < a.sp.max_steps) {
+    while (t_le(m, t1) && step < a.sp.max_steps) {
         ++step;
         hmin_fail |= step_member(m, a.sp, t1, c) != 0;
 #if CLODE_FEATURE_STORE
@@ -635,7 +652,7 @@ __device__ __forceinline__ void features_member(Observer &o, const Args &a, int 
         a.status[i] = member_status_bits(m, step, a, t1, hmin_fail, terminal);
 }
 
-extern "C" __global__ void clode_features(const Args a)
+extern "C" __global__ void CLODE_CAP clode_features(const Args a)
 {
     Counters c = {0, 0, 0, 0};
     int i = a.i_begin + blockIdx.x * blockDim.x + threadIdx.x;
@@ -658,7 +675,7 @@ extern "C" __global__ void clode_features(const Args a)
 // passes stay converged on the expensive part of the loop, and a rejected
 // adaptive attempt is retried in the next iteration instead of holding the
 // warp for a repeat.
-extern "C" __global__ void clode_features_persistent(const Args a)
+extern "C" __global__ void CLODE_CAP clode_features_persistent(const Args a)
 {
     Counters c = {0, 0, 0, 0};
     const unsigned long long t_start = globaltimer_ns();
@@ -730,7 +747,7 @@ extern "C" __global__ void clode_features_persistent(const Args a)
         }
         bool running = true;
         for (int k = 0; k < CLODE_STEP_BLOCK && running; ++k) {
-            running = sc.retry || (step < a.sp.max_steps && (warm ? m.t < t1 : m.t <= t1));
+            running = sc.retry || (step < a.sp.max_steps && (warm ? t_lt(m, t1) : t_le(m, t1)));
             if (!running)
                 break;
             if (!sc.retry)
@@ -778,6 +795,354 @@ extern "C" __global__ void clode_features_persistent(const Args a)
     }
     flush_counters(a, c);
 }
+
+#if !CLODE_FEATURE_STORE
+// ---------------------------------------------- replay of the warm-up pass --
+// A two-pass observer's feature pass integrates exactly the trajectory its
+// warm-up pass integrated (the same start, step sizes and noise: the warm-up
+// writes neither dt nor the RNG words back, initializeObserver.cl:57-77).
+// Instead of integrating it twice, the recording warm-up launch stores every
+// step of the feature pass — the warm-up's steps and, when the warm-up ends
+// exactly on t1, the steps the feature pass's `t <= t1` loop takes beyond
+// it — and the replay launch feeds them to the observer's feature-pass hooks
+// without integrating.  Per member the hooks see the values the feature
+// pass would compute, in the same order, so the features, final state, step
+// size and RNG words are those of the feature pass.
+//
+// Rows are warp-wide: in iteration `row` of the recording launch every lane
+// of a warp with an accepted step stores it in column `lane`, one
+// coalesced 32-lane store per field.  The replay launch has one warp per
+// region and walks its rows in order, each lane following the members its
+// recording lane held.
+#define CLODE_REC_FIELDS (1 + 2 * N_VAR + N_AUX)
+
+// a member's state at the end of its feature pass
+struct Finish {
+    realtype t, dt;
+    realtype x[N_VAR];
+    unsigned long long s0, s1;  // RNG words (stochastic stepper)
+    unsigned int steps;         // the feature pass's step counter (the status word's max_steps test)
+    unsigned int records;       // stored steps
+    unsigned int flags;         // FIN_*
+    unsigned int pad;
+};
+enum { FIN_COMPLETE = 1, FIN_HMIN_FAIL = 2 };
+static_assert(sizeof(Finish) % 4 == 0, "finish block must be a whole number of 32-bit words");
+#define CLODE_FIN_WORDS ((int)(sizeof(Finish) / 4))
+#define CLODE_FIN_VEC ((CLODE_FIN_WORDS + 3) / 4)
+#define CLODE_FIN_STRIDE (4 * CLODE_FIN_VEC)
+
+// read by the host to size the finish blocks (words per member, padding included)
+extern "C" __device__ const unsigned int clode_finish_words = CLODE_FIN_STRIDE;
+// record fields per step, read by the host to size the regions
+extern "C" __device__ const unsigned int clode_record_fields = CLODE_REC_FIELDS;
+
+__device__ __forceinline__ void fin_store(const Finish &f, const Args &a, int i)
+{
+    uint4 *dst = reinterpret_cast<uint4 *>(a.fin + (unsigned long long)i * CLODE_FIN_STRIDE);
+    uint4 v[CLODE_FIN_VEC];
+    v[CLODE_FIN_VEC - 1] = make_uint4(0u, 0u, 0u, 0u);
+    memcpy(v, &f, sizeof(Finish));
+#pragma unroll
+    for (int k = 0; k < CLODE_FIN_VEC; ++k)
+        dst[k] = v[k];
+}
+
+__device__ __forceinline__ void fin_load(Finish &f, const Args &a, int i)
+{
+    const uint4 *src = reinterpret_cast<const uint4 *>(a.fin + (unsigned long long)i * CLODE_FIN_STRIDE);
+    uint4 v[CLODE_FIN_VEC];
+#pragma unroll
+    for (int k = 0; k < CLODE_FIN_VEC; ++k)
+        v[k] = src[k];
+    memcpy(&f, v, sizeof(Finish));
+}
+
+__device__ __forceinline__ void fallback_push(const Args &a, int i)
+{
+    a.fallback[atomicAdd(a.fallback_count, 1u)] = i;
+}
+
+// Warm-up pass of the two-pass observers (clode_init_observer_persistent's
+// member loop, per member the same steps and hooks) that also records the
+// feature pass's steps.  All lanes of a warp iterate together (a lane
+// without a step leaves a hole in its column), so every row holds one step
+// or none per lane.  A warp takes no new member once rec_fetch_rows rows
+// are recorded or its member list is nearly full; the host launches again
+// for the members left.  A member whose steps did not all fit in the region,
+// or that takes no step, is not replayed: it goes to the fallback list and
+// the plain feature pass runs it from the parked observer state.
+extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long R = a.rec_rows;
+    unsigned long long row = 0;  // warp-uniform
+    unsigned int starts = 0;     // warp-uniform: members started in this region
+    bool recording = true;       // warp-uniform: false once the region is full
+    bool exhausted = false;
+    int i = -1;
+    bool fresh = false, tail = false, first = false, complete = false, hmin_fail = false;
+    unsigned int step = 0, records = 0;
+    realtype t1 = ZERO;
+    Member m;
+    Observer o;
+    StepCtl sc;
+    sc.retry = false;
+    for (;;) {
+        const bool want = i < 0 && !exhausted && recording && row < a.rec_fetch_rows &&
+                          starts + 32u <= a.rec_members;
+        const int got = fetch_member(a, want);
+        if (want) {
+            if (got < 0) {
+                exhausted = true;
+            } else {
+                i = got;
+                fresh = true;
+            }
+        }
+        if (__all_sync(0xffffffffu, i < 0))
+            break;
+        if (fresh) {
+            member_load(m, a, i, c);
+            o.init(m.t, m.x, m.dx, m.aux, a.op);
+            step = 0;
+            records = 0;
+            t1 = member_t1(a, i);
+            fresh = tail = hmin_fail = false;
+            first = true;
+            complete = recording;
+        }
+        bool running = i >= 0;
+        for (int k = 0; k < CLODE_STEP_BLOCK; ++k) {
+            if (!__any_sync(0xffffffffu, running))
+                break;
+            bool valid = false;
+            if (running) {
+                // the warm-up pass runs while t < t1; the feature pass while
+                // t <= t1, so it may take steps beyond the warm-up's last one
+                bool go = sc.retry || (step < a.sp.max_steps && (tail ? t_le(m, t1) : t_lt(m, t1)));
+                if (!go && !tail) {
+                    tail = true;
+                    go = step < a.sp.max_steps && t_le(m, t1);
+                }
+                running = go;
+                if (go) {
+                    if (!sc.retry)
+                        ++step;
+                    const int flag = step_attempt(m, a.sp, t1, c, sc);
+                    if (flag != 1) {
+                        valid = true;
+                        hmin_fail |= flag != 0;
+                        if (!tail)
+                            o.warmup(m.t, m.x, m.dx, m.aux, a.op);
+                    }
+                }
+            }
+            if (recording && row >= R)
+                recording = false;
+            if (recording) {
+                const unsigned int vmask = __ballot_sync(0xffffffffu, valid);
+                const unsigned int smask = __ballot_sync(0xffffffffu, valid && first);
+                const unsigned long long cell = warp * R + row;
+                if (valid) {
+                    realtype *r = a.rec + cell * (CLODE_REC_FIELDS * 32ull) + lane;
+                    r[0] = m.t;
+#pragma unroll
+                    for (int j = 0; j < N_VAR; ++j)
+                        r[(1 + j) * 32] = m.x[j];
+#pragma unroll
+                    for (int j = 0; j < N_VAR; ++j)
+                        r[(1 + N_VAR + j) * 32] = m.dx[j];
+#pragma unroll
+                    for (int j = 0; j < N_AUX; ++j)
+                        r[(1 + 2 * N_VAR + j) * 32] = m.aux[j];
+                    ++records;
+                    if (first) {
+                        a.rec_member[warp * a.rec_members + starts + __popc(smask & ((1u << lane) - 1u))] = i;
+                        first = false;
+                    }
+                }
+                if (lane == 0) {
+                    a.rec_mask[2 * cell] = vmask;
+                    a.rec_mask[2 * cell + 1] = smask;
+                }
+                starts += __popc(smask);
+                ++row;
+            } else if (valid) {
+                complete = false;  // a step the region had no room for
+            }
+        }
+        if (i >= 0 && !running) {
+            // the finish block is written for every member, so that the replay
+            // never reads one left by an earlier run
+            const bool replayable = complete && records > 0;
+            Finish f;
+            f.t = m.t;
+            f.dt = m.dt;
+#pragma unroll
+            for (int j = 0; j < N_VAR; ++j)
+                f.x[j] = m.x[j];
+            f.s0 = m.r.s0;
+            f.s1 = m.r.s1;
+            f.steps = step;
+            f.records = records;
+            f.flags = replayable ? (FIN_COMPLETE | (hmin_fail ? FIN_HMIN_FAIL : 0)) : 0u;
+            f.pad = 0;
+            fin_store(f, a, i);
+            if (!replayable)
+                fallback_push(a, i);
+            // rewind to the initial state and arm (clode_init_observer_persistent)
+            m.t = member_t0(a, i);
+            m.tlo = ZERO;
+            load_x0(m.x, a, i);
+            getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
+            c.rhs += 1;
+            o.arm(m.t, m.x, m.dx, m.aux, a.op);
+            park_store(o, a, i);
+            i = -1;
+        }
+    }
+    if (lane == 0)
+        a.rec_used[warp] = (unsigned int)(row < R ? row : R);
+    flush_counters(a, c);
+}
+
+// L2 prefetch of a contiguous global range (TMA bulk prefetch; 16-byte
+// aligned start, size a multiple of 16 bytes)
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned int bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// rows ahead of the replay that are prefetched into L2, in blocks of this many rows
+#ifndef CLODE_REPLAY_AHEAD
+#define CLODE_REPLAY_AHEAD 8
+#endif
+#define CLODE_REPLAY_PF_ROWS 4
+
+// The replay kernel is bound by memory latency and the observer's work, not
+// by occupancy alone: its own register cap keeps the observer state in
+// registers (no local-memory spills).
+#ifndef CLODE_REPLAY_MAXNREG
+#if defined(CLODE_DOUBLE_PRECISION)
+#define CLODE_REPLAY_MAXNREG 255
+#elif CLODE_PRECISE
+#define CLODE_REPLAY_MAXNREG 216
+#else
+#define CLODE_REPLAY_MAXNREG 128
+#endif
+#endif
+
+// Feature pass by replay: one warp per region of the recording launch (the
+// same grid), each lane walking its column.  A member starts where its lane
+// recorded its first step, with the observer state parked (armed) by the
+// recording launch; it ends at its last stored step with the feature pass's
+// final state from its finish block.  A member whose observer ends it early
+// (its event limit) goes to the fallback list, since the state at that step
+// was not stored whole.  The rows a few steps ahead are prefetched into L2.
+extern "C" __global__ void __maxnreg__(CLODE_REPLAY_MAXNREG) clode_features_replay(const Args a)
+{
+    Counters c = {0, 0, 0, 0};
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long R = a.rec_rows;
+    const unsigned long long rows = a.rec_used[warp];
+    const unsigned long long n = (unsigned long long)a.nPts;
+    const unsigned int row_bytes = CLODE_REC_FIELDS * 32u * (unsigned int)sizeof(realtype);
+    unsigned int starts = 0;
+    int i = -1;
+    unsigned int left = 0, events = 0;
+    Observer o;
+    // the first rows of the region into L2 (R is a multiple of 16, so every
+    // region's masks start on a 16-byte boundary)
+    if (lane == 0) {
+        const unsigned long long first = rows < CLODE_REPLAY_AHEAD ? rows : CLODE_REPLAY_AHEAD;
+        if (first > 0) {
+            prefetch_l2(a.rec + warp * R * (CLODE_REC_FIELDS * 32ull), (unsigned int)first * row_bytes);
+            prefetch_l2(a.rec_mask + 2 * warp * R, (unsigned int)((first * 8 + 15) / 16 * 16));
+        }
+    }
+    for (unsigned long long row = 0; row < rows; ++row) {
+        const unsigned long long cell = warp * R + row;
+        // keep CLODE_REPLAY_AHEAD rows in flight: every CLODE_REPLAY_PF_ROWS rows,
+        // the block that far ahead (within the rows recorded)
+        if (lane == 0 && row % CLODE_REPLAY_PF_ROWS == 0) {
+            const unsigned long long ahead = row + CLODE_REPLAY_AHEAD;
+            if (ahead < rows) {
+                const unsigned long long cnt =
+                    rows - ahead < CLODE_REPLAY_PF_ROWS ? rows - ahead : CLODE_REPLAY_PF_ROWS;
+                prefetch_l2(a.rec + (cell + CLODE_REPLAY_AHEAD) * (CLODE_REC_FIELDS * 32ull),
+                            (unsigned int)cnt * row_bytes);
+                // the masks: 8 bytes per row, rounded to whole 16-byte pieces
+                const unsigned long long b0 = (2 * (cell + CLODE_REPLAY_AHEAD) * 4) & ~15ull;
+                const unsigned long long b1 = (2 * (cell + CLODE_REPLAY_AHEAD + cnt) * 4 + 15) & ~15ull;
+                prefetch_l2(reinterpret_cast<const char *>(a.rec_mask) + b0, (unsigned int)(b1 - b0));
+            }
+        }
+        const unsigned int vmask = a.rec_mask[2 * cell];
+        const unsigned int smask = a.rec_mask[2 * cell + 1];
+        if ((smask >> lane) & 1u) {
+            const int j = a.rec_member[warp * a.rec_members + starts + __popc(smask & ((1u << lane) - 1u))];
+            const Finish *fj = reinterpret_cast<const Finish *>(a.fin + (unsigned long long)j * CLODE_FIN_STRIDE);
+            i = -1;
+            if (fj->flags & FIN_COMPLETE) {
+                i = j;
+                left = fj->records;
+                events = 0;
+                park_load(o, a, i);
+            }
+        }
+        starts += __popc(smask);
+        if (i < 0 || !((vmask >> lane) & 1u))
+            continue;
+        const realtype *r = a.rec + cell * (CLODE_REC_FIELDS * 32ull) + lane;
+        const realtype t = r[0];
+        realtype x[N_VAR], dx[N_VAR], aux[NA1];
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            x[j] = r[(1 + j) * 32];
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            dx[j] = r[(1 + N_VAR + j) * 32];
+#pragma unroll
+        for (int j = 0; j < NA1; ++j)
+            aux[j] = j < N_AUX ? r[(1 + 2 * N_VAR + j) * 32] : ZERO;
+        o.update(t, x, dx, aux, a.op);
+        if (o.event(t, x, dx, aux, a.op)) {
+            ++events;
+            if (o.on_event(t, x, dx, aux, a.op)) {
+                fallback_push(a, i);
+                i = -1;
+                continue;
+            }
+        }
+        if (--left == 0) {
+            Finish f;
+            fin_load(f, a, i);
+            FOut out = {a.F, n, i, 0};
+            o.write(out);
+            o.rebase(f.t - member_t0(a, i));
+#pragma unroll
+            for (int j = 0; j < N_VAR; ++j)
+                a.xf[j * n + i] = f.x[j];
+#if CLODE_STOCHASTIC
+            a.rng[i] = f.s0;
+            a.rng[n + i] = f.s1;
+#endif
+            a.dt[i] = f.dt;
+            a.tf[i] = f.t;
+            park_store(o, a, i);
+            if (a.status)
+                a.status[i] = status_bits(f.t, f.x, f.steps, a, member_t1(a, i), (f.flags & FIN_HMIN_FAIL) != 0, false);
+            c.events += events;
+            i = -1;
+        }
+    }
+    flush_counters(a, c);
+}
+#endif  // !CLODE_FEATURE_STORE
 #endif  // CLODE_HAVE_OBSERVER
 
 }  // namespace clode

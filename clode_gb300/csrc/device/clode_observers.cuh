@@ -60,6 +60,88 @@ __device__ __forceinline__ void mean_count(realtype &mean, realtype v, unsigned 
         mean += (v - mean) / (realtype)n;
 }
 
+// Event times.  The precise option (CLODE_PRECISE) refines the time of a
+// threshold crossing inside the step that detected it and keeps event times
+// in FP64, so that periods are differences of FP64 times; otherwise an event
+// happens at the step's time, as in the reference.
+#if CLODE_PRECISE
+typedef double evtime;
+#else
+typedef realtype evtime;
+#endif
+
+// cubic Hermite basis on the step (s in [0, 1]) and its derivative in s
+struct Hermite {
+    double h00, h10, h01, h11, d00, d10, d01, d11;
+    __device__ __forceinline__ void at(double s)
+    {
+        const double s2 = s * s, s3 = s2 * s;
+        h00 = 2.0 * s3 - 3.0 * s2 + 1.0;
+        h10 = s3 - 2.0 * s2 + s;
+        h01 = -2.0 * s3 + 3.0 * s2;
+        h11 = s3 - s2;
+        d00 = 6.0 * s2 - 6.0 * s;
+        d10 = 3.0 * s2 - 4.0 * s + 1.0;
+        d01 = -6.0 * s2 + 6.0 * s;
+        d11 = 3.0 * s2 - 2.0 * s;
+    }
+    // value and s-derivative of the interpolant of (x0, slope d0) -> (x1, d1) over a step h
+    __device__ __forceinline__ double f(double x0, double d0, double x1, double d1, double h) const
+    {
+        return h00 * x0 + h10 * h * d0 + h01 * x1 + h11 * h * d1;
+    }
+    __device__ __forceinline__ double df(double x0, double d0, double x1, double d1, double h) const
+    {
+        return d00 * x0 + d10 * h * d0 + d01 * x1 + d11 * h * d1;
+    }
+};
+
+// Safeguarded Newton (FP64) for the root of g on [0, 1], g(0) and g(1) of
+// opposite signs: g(s) and g'(s) come from g(s, dg).  Starts from s0.
+template <typename G>
+__device__ __forceinline__ double refine_root(G g, double g0, double s0)
+{
+    double lo = 0.0, hi = 1.0;
+    double s = fmin(fmax(s0, 0.0), 1.0);
+    const bool neg0 = g0 < 0.0;
+#pragma unroll 1
+    for (int it = 0; it < 12; ++it) {
+        double dg = 0.0;
+        const double v = g(s, dg);
+        if (v == 0.0)
+            return s;
+        if ((v < 0.0) == neg0)
+            lo = s;
+        else
+            hi = s;
+        double sn = dg != 0.0 ? s - v / dg : 0.5 * (lo + hi);
+        if (!(sn > lo && sn < hi))
+            sn = 0.5 * (lo + hi);
+        if (fabs(sn - s) < 1e-15)
+            return sn;
+        s = sn;
+    }
+    return s;
+}
+
+// time in (t0, t1] at which the interpolant of one variable reaches `level`
+// (x0 on one side of it, x1 on the other)
+__device__ __forceinline__ evtime crossing_time(realtype t0, realtype x0, realtype d0, realtype t1, realtype x1,
+                                                realtype d1, realtype level)
+{
+    const double h = (double)t1 - (double)t0;
+    const double X0 = x0, X1 = x1, D0 = d0, D1 = d1, L = level;
+    const double g0 = X0 - L;
+    auto g = [&](double s, double &dg) {
+        Hermite H;
+        H.at(s);
+        dg = H.df(X0, D0, X1, D1, h);
+        return H.f(X0, D0, X1, D1, h) - L;
+    };
+    const double s = refine_root(g, g0, X1 != X0 ? (L - X0) / (X1 - X0) : 0.5);
+    return (evtime)((double)t0 + s * h);
+}
+
 // first-occurrence arg-extremum of three values, clODE_utilities.cl:49-127
 __device__ __forceinline__ int argmax3(realtype a, realtype b, realtype c)
 {
@@ -125,9 +207,17 @@ struct SolBuf {
 };
 
 // whole-trajectory extent of every state variable, its slope and every aux
+// The time-weighted means follow the reference's running update; the
+// precise option instead keeps the compensated sums of value x step (hi part
+// in xmean / amean, low part in xlo / alo) and divides by the elapsed time
+// when the means are read (xm, am).
 struct Extent {
     realtype xmax[N_VAR], xmin[N_VAR], xmean[N_VAR], dxmax[N_VAR], dxmin[N_VAR];
     realtype amax[NA1], amin[NA1], amean[NA1];
+#if CLODE_PRECISE
+    realtype xlo[N_VAR], alo[NA1];
+    realtype span;  // elapsed time at the last update
+#endif
     __device__ __forceinline__ void reset()
     {
 #pragma unroll
@@ -139,6 +229,15 @@ struct Extent {
         for (int j = 0; j < N_AUX; ++j) {
             amax[j] = -BIG_REAL; amin[j] = BIG_REAL; amean[j] = ZERO;
         }
+#if CLODE_PRECISE
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            xlo[j] = ZERO;
+#pragma unroll
+        for (int j = 0; j < NA1; ++j)
+            alo[j] = ZERO;
+        span = ZERO;
+#endif
     }
     __device__ __forceinline__ void update(const realtype (&x)[N_VAR], const realtype (&dx)[N_VAR],
                                            const realtype (&aux)[NA1], realtype dt, realtype elapsed)
@@ -147,7 +246,14 @@ struct Extent {
         for (int j = 0; j < N_VAR; ++j) {
             xmax[j] = fmax(x[j], xmax[j]);
             xmin[j] = fmin(x[j], xmin[j]);
+#if CLODE_PRECISE
+            CSum cs = {xmean[j], xlo[j]};
+            cs.add_prod(x[j], dt);
+            xmean[j] = cs.hi;
+            xlo[j] = cs.lo;
+#else
             xmean[j] = mean_time(xmean[j], x[j], dt, elapsed);
+#endif
             dxmax[j] = fmax(dx[j], dxmax[j]);
             dxmin[j] = fmin(dx[j], dxmin[j]);
         }
@@ -155,8 +261,35 @@ struct Extent {
         for (int j = 0; j < N_AUX; ++j) {
             amax[j] = fmax(aux[j], amax[j]);
             amin[j] = fmin(aux[j], amin[j]);
+#if CLODE_PRECISE
+            CSum cs = {amean[j], alo[j]};
+            cs.add_prod(aux[j], dt);
+            amean[j] = cs.hi;
+            alo[j] = cs.lo;
+#else
             amean[j] = mean_time(amean[j], aux[j], dt, elapsed);
+#endif
         }
+#if CLODE_PRECISE
+        span = elapsed;
+#endif
+    }
+    // the time-weighted means as written to the features
+    __device__ __forceinline__ realtype xm(int j) const
+    {
+#if CLODE_PRECISE
+        return span != ZERO ? (realtype)(((double)xmean[j] + (double)xlo[j]) / (double)span) : ZERO;
+#else
+        return xmean[j];
+#endif
+    }
+    __device__ __forceinline__ realtype am(int j) const
+    {
+#if CLODE_PRECISE
+        return span != ZERO ? (realtype)(((double)amean[j] + (double)alo[j]) / (double)span) : ZERO;
+#else
+        return amean[j];
+#endif
     }
 };
 
@@ -240,11 +373,11 @@ struct Observer {
     {
 #pragma unroll
         for (int j = 0; j < N_VAR; ++j) {
-            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xmean[j]); o(ext.dxmax[j]); o(ext.dxmin[j]);
+            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xm(j)); o(ext.dxmax[j]); o(ext.dxmin[j]);
         }
 #pragma unroll
         for (int j = 0; j < N_AUX; ++j) {
-            o(ext.amax[j]); o(ext.amin[j]); o(ext.amean[j]);
+            o(ext.amax[j]); o(ext.amin[j]); o(ext.am(j));
         }
         o((realtype)steps);
     }
@@ -329,11 +462,11 @@ struct Observer {
         o(two ? amp.hi : ZERO); o(two ? amp.lo : ZERO); o(two ? amp.mean : ZERO);
 #pragma unroll
         for (int j = 0; j < N_VAR; ++j) {
-            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xmean[j]); o(ext.dxmax[j]); o(ext.dxmin[j]);
+            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xm(j)); o(ext.dxmax[j]); o(ext.dxmin[j]);
         }
 #pragma unroll
         for (int j = 0; j < N_AUX; ++j) {
-            o(ext.amax[j]); o(ext.amin[j]); o(ext.amean[j]);
+            o(ext.amax[j]); o(ext.amin[j]); o(ext.am(j));
         }
 #pragma unroll
         for (int j = 0; j < N_STORE_EVENTS; ++j) {
@@ -478,7 +611,8 @@ struct Observer {
     realtype xrange[N_VAR];
     realtype tex_list[NSE1];
     Stat3 npk, period, hstat;
-    realtype t_start, t_last_event, x_thresh;
+    realtype t_start, x_thresh;
+    evtime t_last_event, t_ev;  // t_ev: the refined time of the current event (precise option)
     unsigned int peaks_now, have_c, inside, events, steps;
 
     __device__ __forceinline__ void init(CLODE_HOOK_ARGS)
@@ -494,7 +628,7 @@ struct Observer {
         for (int j = 0; j < NSE1; ++j)
             tex_list[j] = ZERO;
         npk.reset(); period.reset(); hstat.reset();
-        t_start = t; t_last_event = ZERO; x_thresh = ZERO;
+        t_start = t; t_last_event = ZERO; t_ev = ZERO; x_thresh = ZERO;
         peaks_now = 0; have_c = 0; inside = 0; events = 0; steps = 0;
     }
     // first pass: extent of every state variable
@@ -549,19 +683,50 @@ struct Observer {
         }
         unsigned int was_inside = inside;
         inside = sqrt(acc) < op.nHoodRadius;
-        return was_inside && !inside;
+        const bool exit = was_inside && !inside;
+#if CLODE_PRECISE
+        if (exit) {
+            // the time in this step at which the interpolated state leaves the ball
+            const double h = (double)b.t2 - (double)b.t1, r = op.nHoodRadius;
+            auto g = [&](double s, double &dg) {
+                Hermite H;
+                H.at(s);
+                double v = -r * r;
+                dg = 0.0;
+#pragma unroll
+                for (int j = 0; j < N_VAR; ++j) {
+                    const double R = xrange[j];
+                    const double u = (H.f(b.x1[j], b.d1[j], b.x2[j], b.d2[j], h) - (double)c[j]) / R;
+                    v += u * u;
+                    dg += 2.0 * u * H.df(b.x1[j], b.d1[j], b.x2[j], b.d2[j], h) / R;
+                }
+                return v;
+            };
+            double dg0 = 0.0, dg1 = 0.0;
+            const double g0 = g(0.0, dg0);
+            const double g1 = g(1.0, dg1);
+            const double s = refine_root(g, g0, g1 != g0 ? -g0 / (g1 - g0) : 0.5);
+            t_ev = (double)b.t1 + s * h;
+        }
+#endif
+        return exit;
     }
     __device__ __forceinline__ bool on_event(CLODE_HOOK_ARGS)
     {
+#if CLODE_PRECISE
+        const evtime te = t_ev;
+#else
+        const evtime te = t;
+#endif
         ++events;
         if (events > 1) {
             npk.push((realtype)peaks_now, events - 1);
-            period.push(t - t_last_event, events - 1);
+            period.push((realtype)(te - t_last_event), events - 1);
         }
-        t_last_event = t;
+        t_last_event = te;
         peaks_now = 0;
         if (events <= N_STORE_EVENTS)
-            put(tex_list, events - 1, t);
+            put(tex_list, events - 1, (realtype)te);
         return events == op.maxEventCount;
     }
     __device__ __forceinline__ void write(FOut &o) const
@@ -571,12 +736,12 @@ struct Observer {
         o(two ? npk.hi : ZERO); o(two ? npk.lo : ZERO); o(two ? npk.mean : ZERO);
 #pragma unroll
         for (int j = 0; j < N_VAR; ++j) {
-            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xmean[j]); o(xrange[j]); o(c[j]);
+            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xm(j)); o(xrange[j]); o(c[j]);
             o(ext.dxmax[j]); o(ext.dxmin[j]);
         }
 #pragma unroll
         for (int j = 0; j < N_AUX; ++j) {
-            o(ext.amax[j]); o(ext.amin[j]); o(ext.amean[j]);
+            o(ext.amax[j]); o(ext.amin[j]); o(ext.am(j));
         }
 #pragma unroll
         for (int j = 0; j < N_STORE_EVENTS; ++j)
@@ -603,7 +768,8 @@ struct Observer {
     Stat3 npk, period, updur, downdur, duty, dip, hstat;
     realtype down_mean;
     realtype gxmax, gxmin, gdxmax, gdxmin, x_up, x_down, dx_up, dx_down;
-    realtype t_start, t_last_event, t_down, t_last_max, t_last_min, x_last_min;
+    realtype t_start, t_last_max, t_last_min, x_last_min;
+    evtime t_last_event, t_down, t_ev;  // t_ev: the refined time of the current event (precise option)
     unsigned int peaks_now, steps, events, is_up;
 
     __device__ __forceinline__ void init(CLODE_HOOK_ARGS)
@@ -617,7 +783,7 @@ struct Observer {
         down_mean = ZERO;
         gxmax = -BIG_REAL; gxmin = BIG_REAL; gdxmax = -BIG_REAL; gdxmin = BIG_REAL;
         x_up = ZERO; x_down = ZERO; dx_up = ZERO; dx_down = ZERO;
-        t_start = t; t_last_event = ZERO; t_down = ZERO; t_last_max = ZERO; t_last_min = ZERO;
+        t_start = t; t_last_event = ZERO; t_down = ZERO; t_ev = ZERO; t_last_max = ZERO; t_last_min = ZERO;
         x_last_min = BIG_REAL;
         is_up = 0; peaks_now = 0; steps = 0; events = 0;
     }
@@ -662,14 +828,20 @@ struct Observer {
             }
             if (is_up) {
                 if (sel(x, e) <= x_down && sel(dx, e) >= dx_down) {
+#if CLODE_PRECISE
+                    const realtype xp = sel(b.x1, e);
+                    t_down = xp > x_down ? crossing_time(b.t1, xp, sel(b.d1, e), b.t2, sel(b.x2, e), sel(b.d2, e), x_down)
+                                         : (evtime)t;
+#else
                     t_down = t;
+#endif
                     is_up = 0;
                     if (events > 0 && events <= N_STORE_EVENTS)
-                        put(tdown_list, events - 1, t_down);
+                        put(tdown_list, events - 1, (realtype)t_down);
                     down_mean = sel(x, f);
                 }
             } else {
-                realtype since_down = t - t_down;
+                realtype since_down = (realtype)(t - t_down);
                 if (since_down > ZERO)
                     down_mean = mean_time(down_mean, sel(x, f), h, since_down);
             }
@@ -683,26 +855,40 @@ struct Observer {
             return false;
         if (is_up)
             return false;
-        return sel(x, op.eVarIx) > x_up && sel(dx, op.eVarIx) > dx_up;
+        const bool up = sel(x, op.eVarIx) > x_up && sel(dx, op.eVarIx) > dx_up;
+#if CLODE_PRECISE
+        if (up) {
+            const unsigned int e = op.eVarIx;
+            const realtype xp = sel(b.x1, e);
+            t_ev = xp <= x_up ? crossing_time(b.t1, xp, sel(b.d1, e), b.t2, sel(b.x2, e), sel(b.d2, e), x_up)
+                              : (evtime)t;
+        }
+#endif
+        return up;
     }
     __device__ __forceinline__ bool on_event(CLODE_HOOK_ARGS)
     {
+#if CLODE_PRECISE
+        const evtime te = t_ev;
+#else
+        const evtime te = t;
+#endif
         ++events;
         is_up = 1;
         if (events > 1) {
             unsigned int n = events - 1;
             npk.push((realtype)peaks_now, n);
-            realtype per = t - t_last_event;
+            realtype per = (realtype)(te - t_last_event);
             period.push(per, n);
-            realtype up = t_down - t_last_event;
+            realtype up = (realtype)(t_down - t_last_event);
             updur.push(up, n);
-            downdur.push(t - t_down, n);
+            downdur.push((realtype)(te - t_down), n);
             duty.push(up / per, n);
             dip.push(down_mean - x_last_min, n);
         }
         if (events <= N_STORE_EVENTS)
-            put(tup_list, events - 1, t);
-        t_last_event = t;
+            put(tup_list, events - 1, (realtype)te);
+        t_last_event = te;
         peaks_now = 0;
         return events == op.maxEventCount;
     }
@@ -717,11 +903,11 @@ struct Observer {
         o(two ? dip.hi : ZERO); o(two ? dip.lo : ZERO); o(two ? dip.mean : ZERO);
 #pragma unroll
         for (int j = 0; j < N_VAR; ++j) {
-            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xmean[j]); o(ext.dxmax[j]); o(ext.dxmin[j]);
+            o(ext.xmax[j]); o(ext.xmin[j]); o(ext.xm(j)); o(ext.dxmax[j]); o(ext.dxmin[j]);
         }
 #pragma unroll
         for (int j = 0; j < N_AUX; ++j) {
-            o(ext.amax[j]); o(ext.amin[j]); o(ext.amean[j]);
+            o(ext.amax[j]); o(ext.amin[j]); o(ext.am(j));
         }
 #pragma unroll
         for (int j = 0; j < N_STORE_EVENTS; ++j) {

@@ -16,6 +16,56 @@
 
 namespace clode {
 
+// ------------------------------------------------------- precise option --
+// CLODE_PRECISE = 1 builds the engine's precision option (no counterpart in
+// the reference, not for parity): time accumulated as a compensated pair,
+// the adaptive controller's error estimate as a compensated dot product,
+// compensated time-weighted means and refined event times in the observers.
+// The error-free transformations below use explicitly rounded operations,
+// which the compiler never contracts or reassociates, so they hold in the
+// fmad / fast builds too.
+#ifndef CLODE_PRECISE
+#define CLODE_PRECISE 0
+#endif
+
+// (add_rn and mul_rn come with the RNG, clode_rng.cuh)
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// s + e = a + b exactly (Knuth's TwoSum)
+__device__ __forceinline__ void two_sum(realtype a, realtype b, realtype &s, realtype &e)
+{
+    s = add_rn(a, b);
+    const realtype bp = sub_rn(s, a);
+    e = add_rn(sub_rn(a, sub_rn(s, bp)), sub_rn(b, bp));
+}
+
+// compensated sum (hi, lo): adds v with its rounding error kept in lo
+struct CSum {
+    realtype hi, lo;
+    __device__ __forceinline__ void reset() { hi = ZERO; lo = ZERO; }
+    __device__ __forceinline__ void add(realtype v)
+    {
+        realtype s, e;
+        two_sum(hi, v, s, e);
+        hi = s;
+        lo = add_rn(lo, e);
+    }
+    // adds a * b: the product's rounding error (exact through an fma) joins lo
+    __device__ __forceinline__ void add_prod(realtype a, realtype b)
+    {
+        const realtype p = mul_rn(a, b);
+        const realtype pe = fma_rn(a, b, -p);
+        realtype s, e;
+        two_sum(hi, p, s, e);
+        hi = s;
+        lo = add_rn(lo, add_rn(e, pe));
+    }
+    __device__ __forceinline__ realtype value() const { return add_rn(hi, lo); }
+};
+
 #define NP1 (N_PAR > 0 ? N_PAR : 1)
 #define NA1 (N_AUX > 0 ? N_AUX : 1)
 #define NW1 (N_WIENER > 0 ? N_WIENER : 1)
@@ -28,6 +78,7 @@ namespace clode {
 
 struct Member {
     realtype t, dt;
+    realtype tlo;  // CLODE_PRECISE: the time is t + tlo, |tlo| <= half an ulp of t
     realtype p[NP1];
     realtype x[N_VAR];
     realtype dx[N_VAR];
@@ -46,6 +97,42 @@ struct Counters {
 
 typedef SolverParamsT<realtype> SolverParams;
 
+// the member's time against the end of its span: t < t1 and t <= t1, with
+// the compensated time of the precise option
+__device__ __forceinline__ bool t_lt(const Member &m, realtype t1)
+{
+#if CLODE_PRECISE
+    return m.t < t1 || (m.t == t1 && m.tlo < ZERO);
+#else
+    return m.t < t1;
+#endif
+}
+
+__device__ __forceinline__ bool t_le(const Member &m, realtype t1)
+{
+#if CLODE_PRECISE
+    return m.t < t1 || (m.t == t1 && m.tlo <= ZERO);
+#else
+    return m.t <= t1;
+#endif
+}
+
+// t (+ tlo) advanced by dt: naively as the reference (t += dt), or, precise,
+// as a compensated pair renormalised so that t is the time rounded to
+// working precision
+__device__ __forceinline__ void advance_time(realtype &t, realtype &tlo, realtype dt)
+{
+#if CLODE_PRECISE
+    realtype s, e;
+    two_sum(t, dt, s, e);
+    e = add_rn(e, tlo);
+    t = add_rn(s, e);
+    tlo = sub_rn(e, sub_rn(t, s));
+#else
+    t += dt;
+#endif
+}
+
 #if defined(EXPLICIT_EULER) || defined(STOCHASTIC_EULER) || defined(EXPLICIT_HEUN) || defined(EXPLICIT_RK4)
 #define CLODE_FIXED_STEP 1
 
@@ -57,17 +144,22 @@ typedef SolverParamsT<realtype> SolverParams;
 #define CLODE_RHS_PER_STEP 4
 #endif
 
-__device__ __forceinline__ void fixed_do_step(realtype &t, realtype (&x)[N_VAR], const realtype (&k1)[N_VAR],
-                                              const realtype (&p)[NP1], const realtype dt, realtype (&aux)[NA1],
-                                              const realtype (&w)[NW1])
+__device__ __forceinline__ void fixed_do_step(realtype &t, realtype &tlo, realtype (&x)[N_VAR],
+                                              const realtype (&k1)[N_VAR], const realtype (&p)[NP1],
+                                              const realtype dt, realtype (&aux)[NA1], const realtype (&w)[NW1])
 {
 #if defined(EXPLICIT_EULER) || defined(STOCHASTIC_EULER)
 #pragma unroll
     for (int k = 0; k < N_VAR; ++k)
         x[k] += dt * k1[k];
-    t += dt;
+    advance_time(t, tlo, dt);
 #elif defined(EXPLICIT_HEUN)
+#if CLODE_PRECISE
+    realtype tn = t, tnlo = tlo;
+    advance_time(tn, tnlo, dt);
+#else
     realtype tn = t + dt;
+#endif
     realtype xp[N_VAR], k2[N_VAR];
 #pragma unroll
     for (int k = 0; k < N_VAR; ++k)
@@ -77,11 +169,19 @@ __device__ __forceinline__ void fixed_do_step(realtype &t, realtype (&x)[N_VAR],
     for (int k = 0; k < N_VAR; ++k)
         x[k] += dt * RCONST(0.5) * (k1[k] + k2[k]);
     t = tn;
+#if CLODE_PRECISE
+    tlo = tnlo;
+#endif
 #else
     realtype xs[N_VAR], k2[N_VAR], k3[N_VAR], k4[N_VAR];
     realtype half = dt * RCONST(0.5);
     realtype tm = t + half;
+#if CLODE_PRECISE
+    realtype te = t, telo = tlo;
+    advance_time(te, telo, dt);
+#else
     realtype te = t + dt;
+#endif
 #pragma unroll
     for (int k = 0; k < N_VAR; ++k)
         xs[k] = x[k] + half * k1[k];
@@ -98,13 +198,16 @@ __device__ __forceinline__ void fixed_do_step(realtype &t, realtype (&x)[N_VAR],
     for (int k = 0; k < N_VAR; ++k)
         x[k] += dt * (k1[k] + RCONST(2.0) * k2[k] + RCONST(2.0) * k3[k] + k4[k]) / RCONST(6.0);
     t = te;
+#if CLODE_PRECISE
+    tlo = telo;
+#endif
 #endif
 }
 
 // one fixed step; afterwards m.dx holds f(t_new, x_new) with fresh noise
 __device__ __forceinline__ int step_member(Member &m, const SolverParams &sp, const realtype t1, Counters &c)
 {
-    fixed_do_step(m.t, m.x, m.dx, m.p, m.dt, m.aux, m.w);
+    fixed_do_step(m.t, m.tlo, m.x, m.dx, m.p, m.dt, m.aux, m.w);
 #if CLODE_STOCHASTIC
 #pragma unroll
     for (int j = 0; j < N_WIENER; ++j)
@@ -163,7 +266,17 @@ __device__ __forceinline__ realtype attempt(realtype &t, realtype (&x)[N_VAR], r
     getRHS(tn, x, p, k4, aux, w);
 #pragma unroll
     for (int k = 0; k < N_VAR; ++k) {
+#if CLODE_PRECISE
+        CSum cs;
+        cs.reset();
+        cs.add_prod(e1, k1[k]);
+        cs.add_prod(e2, k2[k]);
+        cs.add_prod(e3, k3[k]);
+        cs.add_prod(e4, k4[k]);
+        err[k] = h * cs.value();
+#else
         err[k] = h * (e1 * k1[k] + e2 * k2[k] + e3 * k3[k] + e4 * k4[k]);
+#endif
         k1[k] = k4[k];
     }
     t = tn;
@@ -226,7 +339,19 @@ __device__ __forceinline__ realtype attempt(realtype &t, realtype (&x)[N_VAR], r
     getRHS(tn, x, p, k7, aux, w);
 #pragma unroll
     for (int k = 0; k < N_VAR; ++k) {
+#if CLODE_PRECISE
+        CSum cs;
+        cs.reset();
+        cs.add_prod(e1, k1[k]);
+        cs.add_prod(e3, k3[k]);
+        cs.add_prod(e4, k4[k]);
+        cs.add_prod(e5, k5[k]);
+        cs.add_prod(e6, k6[k]);
+        cs.add_prod(e7, k7[k]);
+        err[k] = h * cs.value();
+#else
         err[k] = h * (e1 * k1[k] + e3 * k3[k] + e4 * k4[k] + e5 * k5[k] + e6 * k6[k] + e7 * k7[k]);
+#endif
         k1[k] = k7[k];
     }
     t = tn;

@@ -294,8 +294,8 @@ CompiledProgram compile_program(const ProgramSpec &spec)
         opts.push_back("-prec-div=false");
     if (spec.ftz)
         opts.push_back("-ftz=true");
-    if (spec.maxrregcount > 0)
-        opts.push_back("--maxrregcount=" + std::to_string(spec.maxrregcount));
+    if (spec.maxrregcount > 0)  // applied per kernel (clode_kernels.cuh CLODE_CAP)
+        opts.push_back("-DCLODE_MAXNREG=" + std::to_string(spec.maxrregcount));
     if (spec.fast_math)
         opts.push_back("--use_fast_math");
     for (auto &d : spec.defines)

@@ -193,6 +193,9 @@ struct clode_sim {
     DevBuf ev_t, ev_x, ev_dx, ev_aux, nevents;  // features with storage: event states
     DevBuf order, order_scratch;                // persistent kernels: members by decreasing time span
     DevBuf work_counts, order_work;             // warm-up steps per member; the feature pass's order by them
+    // replay of the warm-up pass: record regions, row masks, member lists,
+    // rows used per region, finish blocks, fallback list and its length
+    DevBuf rec, rec_mask, rec_member, rec_used, fin, fallback, fallback_count;
 
     // program
     bool built = false;
@@ -203,6 +206,8 @@ struct clode_sim {
     cudaKernel_t k_transient = nullptr, k_trajectory = nullptr, k_init = nullptr, kp_init = nullptr,
                  k_features = nullptr;
     cudaKernel_t kp_transient = nullptr, kp_trajectory = nullptr, kp_features = nullptr;
+    cudaKernel_t kp_init_rec = nullptr, kp_replay = nullptr;  // replay of the warm-up pass
+    unsigned int fin_words = 0, rec_fields = 0;
     int last_grid = 0, last_block = 0;
     unsigned int obs_words = 0;
     unsigned int built_nse = 0;
@@ -232,6 +237,8 @@ struct clode_sim {
     bool ftz = false;
     bool fast_math = false;
     bool fast_exp = false;        // FP32 exp and controller pow of a few ulp (CLODE_FAST_EXP)
+    bool precise = false;         // precision option (CLODE_PRECISE): compensated time and means,
+                                  // compensated error estimate, refined event times
     bool split_attempts = false;  // persistent kernels: one adaptive attempt per loop iteration
     int step_block = 16;          // persistent kernels: steps between warp-wide refill votes
     int maxrregcount = 0;
@@ -243,6 +250,11 @@ struct clode_sim {
     bool order_by_work = true;  // the feature pass of a two-pass observer takes the members with the
                                 // most warm-up steps first (the separate warm-up launch counts them)
     bool record_work = false;   // the next warm-up launch writes work_counts
+    bool replay = true;         // two-pass observers: the feature pass replays the warm-up's stored steps
+    double replay_mb = 0.0;     // record regions' size in MiB (0: sized to the need, within the free memory)
+    double replay_steps_per_member = 0.0;  // measured by the last replayed run (sizes the next one)
+    int last_replay_chunks = 0;            // recording launches of the last replayed run
+    unsigned int last_fallback = 0;        // members the last replayed run gave to the plain feature pass
     bool use_work_order = false;  // the next features launch runs members in order_work
     long long range_end = -1;  // autotuner trials: run members [0, range_end) only
     int range_stride = 1;      // ... every range_stride-th of them (persistent kernels)
@@ -275,7 +287,8 @@ struct clode_sim {
     {
         return {&x0,  &pars,   &xf,    &rng,    &dt,   &tf,    &tspan_dev, &odata, &F,
                 &t,   &x,      &dx,    &aux,    &nstored, &status, &stats, &stage, &work,
-                &ev_t, &ev_x, &ev_dx, &ev_aux, &nevents, &order, &order_scratch, &work_counts, &order_work};
+                &ev_t, &ev_x, &ev_dx, &ev_aux, &nevents, &order, &order_scratch, &work_counts, &order_work,
+                &rec, &rec_mask, &rec_member, &rec_used, &fin, &fallback, &fallback_count};
     }
 
     size_t real_size() const { return single ? sizeof(float) : sizeof(double); }
@@ -432,6 +445,7 @@ struct clode_sim {
                      "-DN_AUX=" + std::to_string(nAux), "-DN_WIENER=" + std::to_string(nWiener),
                      std::string("-DCLODE_SPLIT_ATTEMPTS=") + (split_attempts ? "1" : "0"),
                      std::string("-DCLODE_FAST_EXP=") + (fast_exp ? "1" : "0"),
+                     std::string("-DCLODE_PRECISE=") + (precise ? "1" : "0"),
                      "-DCLODE_STEP_BLOCK=" + std::to_string(step_block)};
         if (kind == CLODE_SIM_FEATURES) {
             s.defines.push_back("-D" + kObservers.at(observer));
@@ -483,6 +497,7 @@ struct clode_sim {
             check_cuda(cudaLibraryGetKernel(&kp_trajectory, lib, "clode_trajectory_persistent"),
                        "kernel clode_trajectory_persistent");
             k_init = kp_init = k_features = kp_features = nullptr;
+            kp_init_rec = kp_replay = nullptr;
             obs_words = 0;
             if (kind == CLODE_SIM_FEATURES) {
                 check_cuda(cudaLibraryGetKernel(&k_init, lib, "clode_init_observer"), "kernel clode_init_observer");
@@ -495,6 +510,18 @@ struct clode_sim {
                 size_t gb = 0;
                 check_cuda(cudaLibraryGetGlobal(&gp, &gb, lib, "clode_observer_words"), "observer state size");
                 check_cuda(cudaMemcpy(&obs_words, gp, sizeof obs_words, cudaMemcpyDeviceToHost), "observer state size");
+                fin_words = rec_fields = 0;
+                if (!want_store) {
+                    check_cuda(cudaLibraryGetKernel(&kp_init_rec, lib, "clode_init_observer_record"),
+                               "kernel clode_init_observer_record");
+                    check_cuda(cudaLibraryGetKernel(&kp_replay, lib, "clode_features_replay"),
+                               "kernel clode_features_replay");
+                    check_cuda(cudaLibraryGetGlobal(&gp, &gb, lib, "clode_finish_words"), "finish block size");
+                    check_cuda(cudaMemcpy(&fin_words, gp, sizeof fin_words, cudaMemcpyDeviceToHost),
+                               "finish block size");
+                    check_cuda(cudaLibraryGetGlobal(&gp, &gb, lib, "clode_record_fields"), "record size");
+                    check_cuda(cudaMemcpy(&rec_fields, gp, sizeof rec_fields, cudaMemcpyDeviceToHost), "record size");
+                }
             }
         }
         prog = p;
@@ -930,6 +957,12 @@ struct clode_sim {
         double init_ms = 0.0;
         unsigned long long init_stats[CLODE_STAT_COUNT] = {0};
         bool by_work = false;
+        if (!observer_initialized && replay_usable() && features_replay()) {
+            observer_initialized = true;
+            log_msg(CLODE_LOG_DEBUG, "run features (replayed warm-up, %d recording launches, %u members by "
+                                     "the plain feature pass)", last_replay_chunks, last_fallback);
+            return;
+        }
         if (!observer_initialized) {
             if (fuse_init) {
                 fused = 1;
@@ -965,6 +998,223 @@ struct clode_sim {
             last_stats[k] += init_stats[k];
         observer_initialized = true;
         log_msg(CLODE_LOG_DEBUG, "run features");
+    }
+
+
+    // ------------------------------------------------ replayed warm-up --
+    // A two-pass observer's feature pass integrates the trajectory its
+    // warm-up pass already integrated.  With `replay` on, the warm-up launch
+    // (clode_init_observer_record) also stores every step of the feature pass
+    // in per-warp regions of device memory and the feature pass
+    // (clode_features_replay) reads them back instead of integrating again.
+    // The map runs in as many recording + replay launch pairs as the regions
+    // need; members that do not fit, or that the observer ends early, run in
+    // one plain feature-pass launch at the end.  Results are those of the
+    // separate warm-up and feature launches.
+    bool replay_usable() const
+    {
+        return replay && schedule == 1 && !fuse_init && obs_two_pass() && kp_init_rec && kp_replay && kp_features &&
+               !want_store && time_budget_ms <= 0.0 && nPts > 0 && fin_words > 0 && rec_fields > 0;
+    }
+
+    // persistent grid and block of a kernel, as launch() sizes them
+    void persistent_shape(cudaKernel_t k, long long active, unsigned int &grid, unsigned int &block)
+    {
+        int sms = 0;
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count");
+        block = (unsigned int)std::max(32, std::min(1024, block_size)) / 32 * 32;
+        if ((long long)block * sms > active) {
+            const long long per_sm_members = (active + sms - 1) / std::max(sms, 1);
+            const unsigned int b = (unsigned int)std::max<long long>(32, (per_sm_members + 31) / 32 * 32);
+            block = std::min(block, b);
+        }
+        int per_sm = blocks_per_sm;
+        if (per_sm <= 0) {
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k, (int)block, 0),
+                       "occupancy query");
+            per_sm = std::max(per_sm, 1);
+        }
+        const unsigned long long want = (unsigned long long)per_sm * sms;
+        const unsigned long long cover = ((unsigned long long)active + block - 1) / block;
+        grid = (unsigned int)std::max<unsigned long long>(1, std::min(want, cover));
+    }
+
+    template <typename R>
+    void launch_args(cudaKernel_t k, unsigned int grid, unsigned int block, ArgsT<R> &a)
+    {
+        void *params[] = {&a};
+        check_cuda(cudaLaunchKernel((const void *)k, dim3(grid), dim3(block), params, 0, stream), "kernel launch");
+        count_launch();
+    }
+
+    // Region geometry for `budget` bytes over `warps` warps; false when the
+    // budget gives fewer than 64 rows per warp.  Grows the buffers as needed.
+    bool replay_regions(double budget, unsigned long long warps, double row_bytes, size_t rs,
+                        unsigned long long &rows, unsigned int &members_cap)
+    {
+        rows = (unsigned long long)(budget / ((double)warps * (row_bytes + 0.5)));
+        // a multiple of 16 rows: every region's masks start on a 16-byte
+        // boundary, as the replay's bulk L2 prefetches require
+        rows = std::min<unsigned long long>(rows, 0xfffffff0ull) & ~15ull;
+        if (rows < 64)
+            return false;
+        members_cap = (unsigned int)std::min<unsigned long long>(rows / 8 + 64, 0x7fffffffull);
+        rec.reserve((size_t)(warps * rows * rec_fields * 32ull * rs));
+        rec_mask.reserve((size_t)(warps * rows * 2ull * sizeof(unsigned int)) + 16);
+        rec_member.reserve((size_t)(warps * members_cap * sizeof(int)));
+        return true;
+    }
+
+    // false (nothing launched) when the memory for the regions is too small
+    template <typename R>
+    bool replay_run(long long positions)
+    {
+        unsigned int grid = 0, block = 0;
+        persistent_shape(kp_init_rec, positions, grid, block);
+        const unsigned long long warps = (unsigned long long)grid * block / 32;
+        const size_t rs = sizeof(R);
+        // bytes per warp-wide row: every field of 32 lanes and the two masks
+        const double row_bytes = (double)rec_fields * 32.0 * rs + 8.0;
+        // the most the regions may take: the replay_mb option, else most of
+        // the device memory that is free (counting what the regions hold now)
+        double cap;
+        if (replay_mb > 0.0) {
+            cap = replay_mb * 1048576.0;
+        } else {
+            size_t fr = 0, tot = 0;
+            check_cuda(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+            const double held = (double)(rec.bytes + rec_mask.bytes + rec_member.bytes);
+            const double keep = 2.0 * 1073741824.0 + 0.02 * (double)tot;
+            cap = std::max(0.0, ((double)fr + held - keep) * 0.8);
+        }
+        // what `members` members need at `spm` steps each (holes included), plus slack per warp
+        auto need_for = [&](long long members, double spm) {
+            return (double)members * spm * row_bytes / 32.0 * 1.25 + (double)warps * 256.0 * row_bytes;
+        };
+        // first launch: sized from the last run's steps per member, else a modest probe
+        double budget = replay_steps_per_member > 0.0 ? need_for(positions, replay_steps_per_member)
+                                                      : std::max(1073741824.0, 0.05 * cap);
+        budget = std::min(budget, cap);
+        unsigned long long R_rows = 0;
+        unsigned int members_cap = 0;
+        if (!replay_regions(budget, warps, row_bytes, rs, R_rows, members_cap)) {
+            log_msg(CLODE_LOG_INFO, "replay: %.1f MB of device memory gives fewer than 64 rows per warp; "
+                                    "integrating the feature pass", budget / 1e6);
+            return false;
+        }
+        rec_used.reserve((size_t)warps * sizeof(unsigned int));
+        fin.reserve((size_t)nPts * fin_words * sizeof(unsigned int));
+        fallback.reserve((size_t)nPts * sizeof(int));
+        fallback_count.reserve(sizeof(unsigned int));
+        // a warp takes no new member once its region is this full: the members
+        // it holds then must still fit (2.5 times the average member's steps)
+        double spm = replay_steps_per_member;
+        auto fetch_rows_for = [&](unsigned long long rows) {
+            unsigned long long room = rows / 2;
+            if (spm > 0.0)
+                room = std::min<unsigned long long>(room, (unsigned long long)(2.5 * spm) + 64);
+            return rows - room;
+        };
+
+        ArgsT<R> a = make_args<R>();
+        a.fused_init = 0;
+        a.order = member_order();
+        a.work_out = nullptr;
+        a.rec_used = rec_used.as<unsigned int>();
+        a.fin = fin.as<unsigned int>();
+        a.fallback = fallback.as<int>();
+        a.fallback_count = fallback_count.as<unsigned int>();
+        auto set_regions = [&]() {
+            a.rec = rec.as<R>();
+            a.rec_mask = rec_mask.as<unsigned int>();
+            a.rec_member = rec_member.as<int>();
+            a.rec_rows = R_rows;
+            a.rec_fetch_rows = fetch_rows_for(R_rows);
+            a.rec_members = members_cap;
+        };
+        set_regions();
+        check_cuda(cudaMemsetAsync(work.p, 0, sizeof(unsigned int), stream), "work counter reset");
+        check_cuda(cudaMemsetAsync(fallback_count.p, 0, sizeof(unsigned int), stream), "fallback counter reset");
+        last_grid = (int)grid;
+        last_block = (int)block;
+        std::vector<unsigned int> used(warps);
+        unsigned int taken = 0, before = 0;
+        int chunks = 0;
+        for (;;) {
+            launch_args(kp_init_rec, grid, block, a);
+            launch_args(kp_replay, grid, block, a);
+            ++chunks;
+            check_cuda(cudaMemcpyAsync(&taken, work.p, sizeof taken, cudaMemcpyDeviceToHost, stream),
+                       "work counter read");
+            check_cuda(cudaMemcpyAsync(used.data(), rec_used.p, warps * sizeof(unsigned int),
+                                       cudaMemcpyDeviceToHost, stream), "rows read");
+            check_cuda(cudaStreamSynchronize(stream), "replay");
+            const long long done = std::min<long long>(taken, positions);
+            if (done >= positions)
+                break;
+            if (taken == before)
+                fail(CLODE_ERR_INTERNAL, "replay: a recording launch took no member (%u of %lld)", taken, positions);
+            // rows per member of this launch (holes included) estimate the rest
+            double rows_used = 0.0;
+            for (unsigned int u : used)
+                rows_used += u;
+            spm = rows_used * 32.0 / (double)(done - std::min<long long>(before, positions)) / 1.25;
+            const double need = need_for(positions - done, spm);
+            const double have = (double)warps * (double)R_rows * row_bytes;
+            if (need > 1.05 * have && have < 0.95 * cap) {
+                rec.release();
+                rec_mask.release();
+                rec_member.release();
+                if (!replay_regions(std::min(need, cap), warps, row_bytes, rs, R_rows, members_cap))
+                    fail(CLODE_ERR_OUT_OF_MEMORY, "replay: the record regions could not be regrown");
+            }
+            set_regions();
+            before = taken;
+        }
+        unsigned int nfb = 0;
+        check_cuda(cudaMemcpyAsync(&nfb, fallback_count.p, sizeof nfb, cudaMemcpyDeviceToHost, stream),
+                   "fallback count read");
+        check_cuda(cudaStreamSynchronize(stream), "replay");
+        if (nfb > 0) {
+            unsigned int g2 = 0, b2 = 0;
+            persistent_shape(kp_features, (long long)nfb, g2, b2);
+            ArgsT<R> f = make_args<R>();
+            f.fused_init = 0;
+            f.order = fallback.as<int>();
+            f.i_begin = 0;
+            f.i_end = (int)nfb;
+            f.i_stride = 1;
+            check_cuda(cudaMemsetAsync(work.p, 0, sizeof(unsigned int), stream), "work counter reset");
+            launch_args(kp_features, g2, b2, f);
+        }
+        last_replay_chunks = chunks;
+        last_fallback = nfb;
+        if (spm > 0.0)
+            replay_steps_per_member = spm;
+        return true;
+    }
+
+    // the replayed features run; false (nothing run) when it cannot be
+    // given its memory, and the caller integrates the feature pass instead
+    bool features_replay()
+    {
+        begin_run();
+        resize_features();
+        long long active = range_end >= 0 ? std::min(range_end, nPts) : nPts;
+        const long long stride = range_stride > 1 ? range_stride : 1;
+        const long long positions = (active + stride - 1) / stride;
+        const bool ran = single ? replay_run<float>(positions) : replay_run<double>(positions);
+        if (!ran) {
+            last_replay_chunks = 0;
+            last_fallback = 0;
+            check_cuda(cudaStreamSynchronize(stream), "replay");
+            return false;
+        }
+        end_run("features");
+        // average steps per member of this run, to size the next one
+        if (collect_stats && positions > 0)
+            replay_steps_per_member = (double)last_stats[CLODE_STAT_STEPS] / (double)positions;
+        return true;
     }
 
     // Features with storage: the feature pass of features() that also
@@ -1258,6 +1508,12 @@ struct clode_sim {
         snapshot(false);
         // one timed run of the sample, then its dt and RNG words restored
         auto run_trial = [&]() {
+            if (kind == CLODE_SIM_FEATURES && !fuse_init && (ensure_built(), replay_usable()) && features_replay()) {
+                // the path features() takes for this configuration
+                snapshot(true);
+                check_cuda(cudaStreamSynchronize(stream), "autotune restore");
+                return;
+            }
             if (kind == CLODE_SIM_FEATURES) {
                 resize_features();
                 begin_run();
@@ -2034,6 +2290,17 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
             sim->order_by_span = value != 0.0;
         } else if (k == "order_by_work") {
             sim->order_by_work = value != 0.0;
+        } else if (k == "precise") {
+            if ((value != 0.0) != sim->precise) {
+                sim->precise = value != 0.0;
+                sim->built = false;
+            }
+        } else if (k == "replay") {
+            sim->replay = value != 0.0;
+        } else if (k == "replay_mb") {
+            if (value < 0.0)
+                fail(CLODE_ERR_INVALID_ARGUMENT, "replay_mb must be >= 0");
+            sim->replay_mb = value;
         } else {
             fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);
         }
@@ -2062,6 +2329,11 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "collect_stats") *value = sim->collect_stats;
         else if (k == "order_by_span") *value = sim->order_by_span;
         else if (k == "order_by_work") *value = sim->order_by_work;
+        else if (k == "precise") *value = sim->precise;
+        else if (k == "replay") *value = sim->replay;
+        else if (k == "replay_mb") *value = sim->replay_mb;
+        else if (k == "replay_chunks") *value = sim->last_replay_chunks;
+        else if (k == "replay_fallback") *value = sim->last_fallback;
         else if (k == "last_grid") *value = sim->last_grid;
         else if (k == "last_block") *value = sim->last_block;
         else fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);

@@ -232,12 +232,17 @@ def test_split_attempts_bitwise(stepper, kind):
     assert sc.kind == kind
     ref = run_engine(sc, options={"schedule": 0, "fmad": 0})
     assert ref["stats"][0]["rejected"] > 0
-    for opts in ({"schedule": 1, "fmad": 0, "split_attempts": 0}, {"schedule": 1, "fmad": 0, "split_attempts": 1},
-                 {"schedule": 1, "fmad": 0, "split_attempts": 1, "fuse_init": 0}):
+    # the counters match where both runs integrate the same passes; the
+    # replayed feature pass (last options) integrates the trajectory once
+    for opts in ({"schedule": 1, "fmad": 0, "split_attempts": 0, "replay": 0},
+                 {"schedule": 1, "fmad": 0, "split_attempts": 1, "replay": 0},
+                 {"schedule": 1, "fmad": 0, "split_attempts": 1, "fuse_init": 0, "replay": 0},
+                 {"schedule": 1, "fmad": 0, "split_attempts": 1, "fuse_init": 0, "replay": 1}):
         eng = run_engine(sc, options=opts)
         keys = ("xf", "tf", "dt") + (("t", "x", "dx", "n_stored") if kind == "trajectory" else ())
         assert_bitwise(eng, ref, keys=keys)  # and every features run
-        assert eng["stats"][0]["rejected"] == ref["stats"][0]["rejected"]
+        if not (kind == "features" and opts["replay"]):
+            assert eng["stats"][0]["rejected"] == ref["stats"][0]["rejected"]
 
 
 @pytest.mark.parametrize("single", [False, True], ids=["fp64", "fp32"])
