@@ -1081,8 +1081,23 @@ extern "C" __global__ void __maxnreg__(CLODE_REPLAY_MAXNREG) clode_features_repl
                 prefetch_l2(reinterpret_cast<const char *>(a.rec_mask) + b0, (unsigned int)(b1 - b0));
             }
         }
+        // the row's masks and this lane's column are loaded together, before
+        // anything depends on them, so a row costs one memory latency (a
+        // hole in the column is loaded too, and ignored)
         const unsigned int vmask = a.rec_mask[2 * cell];
         const unsigned int smask = a.rec_mask[2 * cell + 1];
+        const realtype *r = a.rec + cell * (CLODE_REC_FIELDS * 32ull) + lane;
+        const realtype t = r[0];
+        realtype x[N_VAR], dx[N_VAR], aux[NA1];
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            x[j] = r[(1 + j) * 32];
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            dx[j] = r[(1 + N_VAR + j) * 32];
+#pragma unroll
+        for (int j = 0; j < NA1; ++j)
+            aux[j] = j < N_AUX ? r[(1 + 2 * N_VAR + j) * 32] : ZERO;
         if ((smask >> lane) & 1u) {
             const int j = a.rec_member[warp * a.rec_members + starts + __popc(smask & ((1u << lane) - 1u))];
             const Finish *fj = reinterpret_cast<const Finish *>(a.fin + (unsigned long long)j * CLODE_FIN_STRIDE);
@@ -1097,18 +1112,6 @@ extern "C" __global__ void __maxnreg__(CLODE_REPLAY_MAXNREG) clode_features_repl
         starts += __popc(smask);
         if (i < 0 || !((vmask >> lane) & 1u))
             continue;
-        const realtype *r = a.rec + cell * (CLODE_REC_FIELDS * 32ull) + lane;
-        const realtype t = r[0];
-        realtype x[N_VAR], dx[N_VAR], aux[NA1];
-#pragma unroll
-        for (int j = 0; j < N_VAR; ++j)
-            x[j] = r[(1 + j) * 32];
-#pragma unroll
-        for (int j = 0; j < N_VAR; ++j)
-            dx[j] = r[(1 + N_VAR + j) * 32];
-#pragma unroll
-        for (int j = 0; j < NA1; ++j)
-            aux[j] = j < N_AUX ? r[(1 + 2 * N_VAR + j) * 32] : ZERO;
         o.update(t, x, dx, aux, a.op);
         if (o.event(t, x, dx, aux, a.op)) {
             ++events;

@@ -261,6 +261,8 @@ struct clode_sim {
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t rev[3] = {nullptr, nullptr, nullptr};  // replayed runs: times of the launch kinds
+    double last_record_ms = 0.0, last_replay_ms = 0.0, last_fallback_ms = 0.0;
     double last_ms = 0.0;
     unsigned long long last_stats[CLODE_STAT_COUNT] = {0};
 
@@ -280,6 +282,9 @@ struct clode_sim {
                 cudaEventDestroy(ev0);
             if (ev1)
                 cudaEventDestroy(ev1);
+            for (cudaEvent_t &e : rev)
+                if (e)
+                    cudaEventDestroy(e);
         }
     }
 
@@ -395,6 +400,11 @@ struct clode_sim {
                 cudaStreamDestroy(stream);
                 cudaEventDestroy(ev0);
                 cudaEventDestroy(ev1);
+                for (cudaEvent_t &e : rev)
+                    if (e) {
+                        cudaEventDestroy(e);
+                        e = nullptr;
+                    }
                 cudaSetDevice(device);
             }
             check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -1140,15 +1150,29 @@ struct clode_sim {
         std::vector<unsigned int> used(warps);
         unsigned int taken = 0, before = 0;
         int chunks = 0;
+        for (cudaEvent_t &e : rev)
+            if (!e)
+                check_cuda(cudaEventCreate(&e), "cudaEventCreate");
+        last_record_ms = last_replay_ms = last_fallback_ms = 0.0;
+        auto elapsed = [&](cudaEvent_t e0, cudaEvent_t e1) {
+            float ms = 0.0f;
+            check_cuda(cudaEventElapsedTime(&ms, e0, e1), "event timing");
+            return (double)ms;
+        };
         for (;;) {
+            check_cuda(cudaEventRecord(rev[0], stream), "event record");
             launch_args(kp_init_rec, grid, block, a);
+            check_cuda(cudaEventRecord(rev[1], stream), "event record");
             launch_args(kp_replay, grid, block, a);
+            check_cuda(cudaEventRecord(rev[2], stream), "event record");
             ++chunks;
             check_cuda(cudaMemcpyAsync(&taken, work.p, sizeof taken, cudaMemcpyDeviceToHost, stream),
                        "work counter read");
             check_cuda(cudaMemcpyAsync(used.data(), rec_used.p, warps * sizeof(unsigned int),
                                        cudaMemcpyDeviceToHost, stream), "rows read");
             check_cuda(cudaStreamSynchronize(stream), "replay");
+            last_record_ms += elapsed(rev[0], rev[1]);
+            last_replay_ms += elapsed(rev[1], rev[2]);
             const long long done = std::min<long long>(taken, positions);
             if (done >= positions)
                 break;
@@ -1185,7 +1209,11 @@ struct clode_sim {
             f.i_end = (int)nfb;
             f.i_stride = 1;
             check_cuda(cudaMemsetAsync(work.p, 0, sizeof(unsigned int), stream), "work counter reset");
+            check_cuda(cudaEventRecord(rev[0], stream), "event record");
             launch_args(kp_features, g2, b2, f);
+            check_cuda(cudaEventRecord(rev[1], stream), "event record");
+            check_cuda(cudaStreamSynchronize(stream), "replay fallback");
+            last_fallback_ms = elapsed(rev[0], rev[1]);
         }
         last_replay_chunks = chunks;
         last_fallback = nfb;
@@ -2334,6 +2362,9 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "replay_mb") *value = sim->replay_mb;
         else if (k == "replay_chunks") *value = sim->last_replay_chunks;
         else if (k == "replay_fallback") *value = sim->last_fallback;
+        else if (k == "replay_record_ms") *value = sim->last_record_ms;
+        else if (k == "replay_replay_ms") *value = sim->last_replay_ms;
+        else if (k == "replay_fallback_ms") *value = sim->last_fallback_ms;
         else if (k == "last_grid") *value = sim->last_grid;
         else if (k == "last_block") *value = sim->last_block;
         else fail(CLODE_ERR_INVALID_ARGUMENT, "unknown option '%s'", key);

@@ -302,9 +302,24 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * spans the persistent lanes take the members in decreasing order of span;
  * results are the same either way), "order_by_work" (0/1, default 1: the
  * feature pass of a two-pass observer takes the members in decreasing order
- * of the steps its separate warm-up launch counted; same results).  Read-only for get_option: "last_grid", "last_block".
+ * of the steps its separate warm-up launch counted; same results),
+ * "replay" (0/1, default 1: with a two-pass observer, the persistent schedule
+ * and separate passes, the warm-up launch stores every step of the feature
+ * pass in device memory and the feature pass replays them into the observer
+ * instead of integrating the trajectory again; results are identical),
+ * "replay_mb" (device memory for the stored steps in MiB; 0, the default:
+ * sized from the previous run's steps per member, at most 80 % of the free
+ * device memory; the map runs in as many launch pairs as that memory needs),
+ * "precise" (0/1, default 0: the precision option, not a parity build:
+ * compensated time accumulation, compensated time-weighted means, the
+ * adaptive error estimate as a compensated sum, event times refined inside
+ * the detecting step in FP64).  Read-only for get_option: "last_grid",
+ * "last_block", and of the last replayed run "replay_chunks" (launch pairs),
+ * "replay_fallback" (members given to the integrated feature pass),
+ * "replay_record_ms", "replay_replay_ms", "replay_fallback_ms" (device time
+ * of each launch kind).
  * Changing a build option (fmad, prec_div, ftz, fast_math, fast_exp, maxrregcount,
- * split_attempts, step_block) recompiles the program at the next run. */
+ * split_attempts, step_block, precise) recompiles the program at the next run. */
 int clode_sim_set_option(clode_sim *sim, const char *key, double value);
 int clode_sim_get_option(clode_sim *sim, const char *key, double *value);
 /* Chains: ops run back to back on the simulator's stream, one synchronisation
