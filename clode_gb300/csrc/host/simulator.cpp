@@ -1101,9 +1101,11 @@ struct clode_sim {
         auto need_for = [&](long long members, double spm) {
             return (double)members * spm * row_bytes / 32.0 * 1.25 + (double)warps * 256.0 * row_bytes;
         };
-        // first launch: sized from the last run's steps per member, else a modest probe
+        // first launch: sized from the last run's steps per member, else a
+        // quarter of what the regions may take (the launches after it are
+        // sized from what it measured)
         double budget = replay_steps_per_member > 0.0 ? need_for(positions, replay_steps_per_member)
-                                                      : std::max(1073741824.0, 0.05 * cap);
+                                                      : std::max(1073741824.0, 0.25 * cap);
         budget = std::min(budget, cap);
         unsigned long long R_rows = 0;
         unsigned int members_cap = 0;
