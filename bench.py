@@ -49,6 +49,21 @@ FLOPS_PER_STEP_OBS = 5 * N_VAR + 3 * N_AUX + 6  # nhood2 per-step extrema and me
 # build on the 512 x 512 case (262,144 members: 76.6 MB + 519.6 MB), scaled
 # by members; the traffic is per-member state, so it grows in proportion
 DRAM_BYTES_PER_MEMBER = (36643072 + 39959552 + 216447488 + 303181824) / 262144
+# the replayed feature pass: bytes of one stored step (t, x, dx, aux in FP32)
+REC_BYTES = (1 + 2 * N_VAR + N_AUX) * 4
+# DRAM bytes (read + write) per member of the recording warm-up launches of a
+# replayed map (ncu, 512 x 512 case, scaled by members; see profiles/)
+REC_DRAM_BYTES_PER_MEMBER = None
+
+
+def measured_hbm_peak() -> tuple[float, str]:
+    """The HBM copy rate of MEASURED_PEAKS.json (GB/s), else the 6.8 TB/s fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        return float(peaks["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback 6.8 TB/s"
 
 
 def make_workload(grid: int, seed: int, tmin: float, tmax: float, rank: int = 0):
@@ -619,7 +634,7 @@ def main():
 
     # device-timed steps, inputs resident in HBM
     launches0 = N.lib.clode_launch_count()
-    kernel_ms, stats = [], []
+    kernel_ms, stats, split = [], [], []
     barrier()
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
@@ -627,6 +642,8 @@ def main():
             sim.features(True)
             kernel_ms.append(sim.last_kernel_ms())
             stats.append(sim.get_stats())
+            split.append({k: sim.get_option(k) for k in ("replay_chunks", "replay_fallback", "replay_record_ms",
+                                                          "replay_replay_ms", "replay_fallback_ms")})
             l2_flush()
         wall_dev = time.perf_counter() - t0
     barrier()
@@ -663,13 +680,33 @@ def main():
 
     st = stats[-1]
     ms = kernel_ms[-1]
+    sp_ = split[-1]
+    hbm_peak, hbm_src = measured_hbm_peak()
+    replayed = sp_["replay_chunks"] > 0
     attempts = st["rhs_evals"] / 6.0
-    flops = st["rhs_evals"] * FLOPS_PER_RHS + attempts * FLOPS_PER_ATTEMPT + st["steps"] * FLOPS_PER_STEP_OBS
-    achieved_tflops = flops / (ms / 1e3) / 1e12
     info = W._device_infos()[local]
     sm_mhz = clk["sm_mhz"] or 1920.0
     peak_tflops = info.compute_units * 128 * 2 * sm_mhz * 1e6 / 1e12
     rhs_per_s = st["rhs_evals"] / (ms / 1e3)
+    if replayed:
+        # the recording warm-up launches integrate (stages, right-hand sides,
+        # controller): FP32-bound; the replay launches read the stored steps
+        # (t, x, dx, aux: REC_BYTES per step) and run the observer: HBM-bound
+        rec_ms = sp_["replay_record_ms"]
+        flops = st["rhs_evals"] * FLOPS_PER_RHS + attempts * FLOPS_PER_ATTEMPT
+        achieved_tflops = flops / (rec_ms / 1e3) / 1e12
+        rep_bytes = st["steps"] * REC_BYTES
+        roof_replay = {"bound": "hbm", "achieved": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9,
+                       "peak": hbm_peak, "unit": "GB/s",
+                       "frac": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9 / hbm_peak,
+                       "traffic": None, "bytes_per_step": REC_BYTES,
+                       "peak_source": hbm_src, "kernel": "clode_features_replay",
+                       "ms": sp_["replay_replay_ms"]}
+    else:
+        rec_ms = ms
+        flops = st["rhs_evals"] * FLOPS_PER_RHS + attempts * FLOPS_PER_ATTEMPT + st["steps"] * FLOPS_PER_STEP_OBS
+        achieved_tflops = flops / (ms / 1e3) / 1e12
+        roof_replay = None
 
     line = {
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
@@ -696,11 +733,16 @@ def main():
         "stats_per_step": st,
         "wall_ms_per_step_device_loop": 1e3 * wall_dev / args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
-                     "frac": achieved_tflops / peak_tflops, "traffic": DRAM_BYTES_PER_MEMBER * n,
-                     "traffic_source": "ncu DRAM bytes of the 512 x 512 map (both launches), scaled by members",
+                     "frac": achieved_tflops / peak_tflops,
+                     "traffic": ((REC_DRAM_BYTES_PER_MEMBER or 0) if replayed else DRAM_BYTES_PER_MEMBER) * n
+                     or None,
+                     "traffic_source": "ncu DRAM bytes of the 512 x 512 map, scaled by members",
                      "peak_source": f"nominal FP32 FMA rate {info.compute_units} SMs x 128 lanes x 2 at the "
                                     f"median sampled SM clock {sm_mhz:.0f} MHz",
-                     "flops_per_launch": flops},
+                     "kernel": "clode_init_observer_record" if replayed else "clode_init_observer + clode_features",
+                     "ms": rec_ms, "flops_per_launch": flops},
+        "roofline_replay": roof_replay,
+        "replay": sp_,
         "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * float(np.mean(e2e_times))},
         "gpu_launches": int(launches_dev + launches_e2e),
