@@ -637,15 +637,16 @@ class SimulatorBase:
 
     def autotune(self, sample: int = 0) -> dict:
         """Pick register cap, block size, (adaptive steppers) the stepping
-        variant and (two-pass observers) fused or separate observer
-        initialisation by timing the persistent kernels on members [0, sample)
-        (no reference counterpart)."""
+        variant and (two-pass observers) the replayed or integrated feature
+        pass and fused or separate observer initialisation, by timing the
+        persistent kernels on a strided sample of ``sample`` members (no
+        reference counterpart)."""
         ms = C.c_double(0.0)
         _check(N.lib.clode_sim_autotune(self._handle, int(sample), C.byref(ms)))
         return {"ms": ms.value, "maxrregcount": int(self.get_option("maxrregcount")),
                 "block_size": int(self.get_option("block_size")),
                 "split_attempts": int(self.get_option("split_attempts")),
-                "fuse_init": int(self.get_option("fuse_init"))}
+                "fuse_init": int(self.get_option("fuse_init")), "replay": int(self.get_option("replay"))}
 
     def kernel_registers(self, kernel: str) -> int:
         r, t = C.c_int(0), C.c_int(0)

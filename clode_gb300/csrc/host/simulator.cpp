@@ -1582,6 +1582,8 @@ struct clode_sim {
         double best = 1e300;
         int best_regs = maxrregcount, best_block = block_size;
         schedule = 1;
+        ensure_built();
+        run_trial();  // untimed: buffers (and the replay's regions) allocated before the timed trials
         for (auto &cd : cands) {
             if (maxrregcount != cd[0]) {
                 maxrregcount = cd[0];
@@ -1616,6 +1618,23 @@ struct clode_sim {
                 split_attempts = base_split;
                 built = false;
             }
+        }
+        // replayed or integrated feature pass (two-pass observers, separate passes)
+        if (kind == CLODE_SIM_FEATURES && obs_two_pass() && !fuse_init) {
+            ensure_built();
+            const bool base_replay = replay;
+            replay = !base_replay;
+            try {
+                run_trial();
+            } catch (...) {
+                replay = base_replay;
+                throw;
+            }
+            log_msg(CLODE_LOG_INFO, "autotune: replay=%d: %.3f ms", (int)replay, last_ms);
+            if (last_ms < best)
+                best = last_ms;
+            else
+                replay = base_replay;
         }
         // fused or separate observer initialisation (two-pass observers)
         if (kind == CLODE_SIM_FEATURES && obs_two_pass()) {
