@@ -419,6 +419,11 @@ def bench_configs(args, tuned_options: dict) -> dict:
     for k, v in tuned_options.items():
         sim.set_option(k, v)
     sim.set_solver_params(W.SolverParams(dt=1e-3, dtmax=1.0, abstol=1e-9, reltol=1e-6, max_steps=1000000))
+    # this map's own tuning (a cheap right-hand side: whether replaying the
+    # stored steps pays is the autotuner's call), on a strided sample
+    sim.set_problem_data(x0.flatten(order="F"), pars.flatten(order="F"))
+    sim.set_tspan([0.0, 500.0])
+    tuned_lorenz = sim.autotune(131072)
     times = []
     for _ in range(3):
         sim.set_problem_data(x0.flatten(order="F"), pars.flatten(order="F"))  # same size: dt continues
@@ -434,7 +439,7 @@ def bench_configs(args, tuned_options: dict) -> dict:
     out["lorenz_dp45_fp32"] = {
         "members": n, "steps": st["steps"], "rejected": st["rejected"], "rhs_evals": st["rhs_evals"], "ms": ms,
         "max_steps": 1000000, "members_at_max_steps": int(((status & 4) != 0).sum()),
-        "members_hmin_fail": int(((status & 1) != 0).sum()),
+        "members_hmin_fail": int(((status & 1) != 0).sum()), "autotune": tuned_lorenz,
         "points_per_s": n / (ms / 1e3), "rhs_evals_per_s": st["rhs_evals"] / (ms / 1e3),
         "roofline": {"bound": "fp32", "achieved": flops / (ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
                      "frac": flops / (ms / 1e3) / 1e12 / peak,
@@ -542,6 +547,9 @@ def main():
                     help="feature pass replays the warm-up's stored steps (engine default 1)")
     ap.add_argument("--replay-mb", type=float, default=None, help="record regions in MiB (engine default: automatic)")
     ap.add_argument("--precise", type=int, default=None, help="the engine's precision option (engine default 0)")
+    ap.add_argument("--replay-stages", type=int, default=None,
+                    help="shared-memory row stages of the replay (-1 automatic, the engine default; 0: rows read "
+                         "from global memory)")
     ap.add_argument("--autotune", type=int, default=1048576,
                     help="autotune on a strided sample of this many members first (0: off)")
     ap.add_argument("--surrogate-grid", type=int, default=4096)
@@ -600,7 +608,7 @@ def main():
                      ("fuse_init", args.fuse_init), ("step_block", args.step_block),
                      ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm),
                      ("order_by_span", args.order_by_span), ("replay", args.replay), ("replay_mb", args.replay_mb),
-                     ("precise", args.precise)):
+                     ("precise", args.precise), ("replay_stages", args.replay_stages)):
         if val is not None:
             sim.set_option(key, val)
     sim.build_cl()
@@ -642,8 +650,9 @@ def main():
             sim.features(True)
             kernel_ms.append(sim.last_kernel_ms())
             stats.append(sim.get_stats())
-            split.append({k: sim.get_option(k) for k in ("replay_chunks", "replay_fallback", "replay_record_ms",
-                                                          "replay_replay_ms", "replay_fallback_ms")})
+            split.append({k: sim.get_option(k) for k in ("replay_chunks", "replay_fallback", "replay_rewarm",
+                                                          "replay_stages_used", "replay_rows", "replay_record_ms",
+                                                          "replay_replay_ms", "replay_fallback_ms", "warmup_ms")})
             l2_flush()
         wall_dev = time.perf_counter() - t0
     barrier()
@@ -700,7 +709,9 @@ def main():
                        "peak": hbm_peak, "unit": "GB/s",
                        "frac": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9 / hbm_peak,
                        "traffic": None, "bytes_per_step": REC_BYTES,
-                       "peak_source": hbm_src, "kernel": "clode_features_replay",
+                       "peak_source": hbm_src,
+                       "kernel": "clode_features_replay_staged" if sp_["replay_stages_used"] >= 2
+                       else "clode_features_replay",
                        "ms": sp_["replay_replay_ms"]}
     else:
         rec_ms = ms
@@ -777,10 +788,30 @@ def main():
                     "frac_period_rel_err_above_1e-4": float(np.mean(r > 1e-4)),
                     "frac_period_rel_err_above_1e-2": float(np.mean(r > 1e-2))}
 
+        # the engine's precise option (FP32 integration, compensated sums,
+        # event times refined in FP64) on the same members and build options
+        ps = W.FeatureSimulatorBase(pi, "dopri5", "nhood2", op, True, res, "")
+        for key in ("fmad", "prec_div", "ftz", "fast_math", "fast_exp", "maxrregcount", "split_attempts",
+                    "schedule", "block_size"):
+            ps.set_option(key, sim.get_option(key))
+        ps.set_option("precise", 1)
+        ps.build_cl()
+        ps.set_solver_params(W.SolverParams(**SOLVER))
+        ps.set_problem_data(np.ascontiguousarray(x0[idx].flatten(order="F")),
+                            np.ascontiguousarray(pars[idx].flatten(order="F")))
+        ps.set_tspan_per_member(np.ascontiguousarray(tspan[idx].ravel()))
+        ps.features(True)
+        Fq = np.asarray(ps.get_f()).reshape(nf, idx.size).T
+        del ps
         line["error_vs_fp64"] = {"reference_run": "CPU oracle, FP64, DP45 rtol = abstol = 1e-10, same members",
-                                 "gpu_fp32": _vs64(Fg), "cpu_fp32": _vs64(Fc)}
+                                 "gpu_fp32": _vs64(Fg), "gpu_fp32_precise": _vs64(Fq), "cpu_fp32": _vs64(Fc)}
     opts = {k: sim.get_option(k) for k in ("schedule", "block_size", "maxrregcount", "fmad", "prec_div", "ftz",
                                            "fast_math", "fast_exp", "split_attempts", "fuse_init")}
+    # the map's simulator (and the device memory of its stored steps) is not
+    # needed by the workloads below
+    del sim
+    import gc
+    gc.collect()
     if rank == 0 and not args.no_surrogate:
         try:
             line["surrogate"] = bench_surrogate(args, opts)

@@ -122,6 +122,11 @@ struct ArgsT {
     unsigned int *fin;
     int *fallback;
     unsigned int *fallback_count;
+    // the replay's shared-memory stages per warp (rows copied ahead by TMA
+    // bulk copies; 0: rows read from global memory), and a word the replay
+    // sets when a stage was not filled within its wait limit
+    unsigned int rec_stages;
+    unsigned int *rec_error;
     SolverParamsT<R> sp;
     ObserverParamsT<R> op;
 };

@@ -813,8 +813,18 @@ extern "C" __global__ void CLODE_CAP clode_features_persistent(const Args a)
 // of a warp with an accepted step stores it in column `lane`, one
 // coalesced 32-lane store per field.  The replay launch has one warp per
 // region and walks its rows in order, each lane following the members its
-// recording lane held.
+// recording lane held.  A row holds, per step, what the observer's
+// warm-up-dependent feature-pass logic reads (Observer::rec_store); the
+// recording launch takes the rest of the feature pass (FeatureSums: extent,
+// means, step statistics) from the same steps and leaves it in the member's
+// finish block.  With the precise option (event times interpolated from
+// every state variable and slope) a row holds t, x, dx and aux and the
+// replay runs the whole update.
+#if defined(CLODE_OBS_SPLIT)
+#define CLODE_REC_FIELDS (Observer::split_fields)
+#else
 #define CLODE_REC_FIELDS (1 + 2 * N_VAR + N_AUX)
+#endif
 
 // a member's state at the end of its feature pass
 struct Finish {
@@ -825,6 +835,9 @@ struct Finish {
     unsigned int records;       // stored steps
     unsigned int flags;         // FIN_*
     unsigned int pad;
+#if defined(CLODE_OBS_SPLIT)
+    FeatureSums fs;  // the feature pass's warm-up-independent accumulators
+#endif
 };
 enum { FIN_COMPLETE = 1, FIN_HMIN_FAIL = 2 };
 static_assert(sizeof(Finish) % 4 == 0, "finish block must be a whole number of 32-bit words");
@@ -858,9 +871,19 @@ __device__ __forceinline__ void fin_load(Finish &f, const Args &a, int i)
     memcpy(&f, v, sizeof(Finish));
 }
 
+// members the plain feature pass finishes from their parked observer state
+// (fallback[0 .. fallback_count[0]))
 __device__ __forceinline__ void fallback_push(const Args &a, int i)
 {
     a.fallback[atomicAdd(a.fallback_count, 1u)] = i;
+}
+
+// members whose warm-up a full region cut short: the plain warm-up and
+// feature passes run them again from the start (fallback[nPts - k], k = 1 ..
+// fallback_count[1], from the end of the same list)
+__device__ __forceinline__ void rewarm_push(const Args &a, int i)
+{
+    a.fallback[(unsigned int)a.nPts - 1u - atomicAdd(a.fallback_count + 1, 1u)] = i;
 }
 
 // Warm-up pass of the two-pass observers (clode_init_observer_persistent's
@@ -869,9 +892,12 @@ __device__ __forceinline__ void fallback_push(const Args &a, int i)
 // without a step leaves a hole in its column), so every row holds one step
 // or none per lane.  A warp takes no new member once rec_fetch_rows rows
 // are recorded or its member list is nearly full; the host launches again
-// for the members left.  A member whose steps did not all fit in the region,
-// or that takes no step, is not replayed: it goes to the fallback list and
-// the plain feature pass runs it from the parked observer state.
+// for the members left.  When the region is full the warp stops: the
+// members it holds then (their steps did not all fit) go, warm-up unfinished,
+// to the list that the plain warm-up and feature passes run again, so that
+// no launch waits on a member far longer than its region.  A member that
+// takes no step goes to the fallback list and the plain feature pass runs it
+// from the parked observer state.
 extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
 {
     Counters c = {0, 0, 0, 0};
@@ -880,19 +906,21 @@ extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
     const unsigned long long R = a.rec_rows;
     unsigned long long row = 0;  // warp-uniform
     unsigned int starts = 0;     // warp-uniform: members started in this region
-    bool recording = true;       // warp-uniform: false once the region is full
+    bool full = false;           // warp-uniform: the region has no row left
     bool exhausted = false;
     int i = -1;
-    bool fresh = false, tail = false, first = false, complete = false, hmin_fail = false;
+    bool fresh = false, tail = false, first = false, hmin_fail = false;
     unsigned int step = 0, records = 0;
     realtype t1 = ZERO;
     Member m;
     Observer o;
+#if defined(CLODE_OBS_SPLIT)
+    FeatureSums fs;
+#endif
     StepCtl sc;
     sc.retry = false;
     for (;;) {
-        const bool want = i < 0 && !exhausted && recording && row < a.rec_fetch_rows &&
-                          starts + 32u <= a.rec_members;
+        const bool want = i < 0 && !exhausted && row < a.rec_fetch_rows && starts + 32u <= a.rec_members;
         const int got = fetch_member(a, want);
         if (want) {
             if (got < 0) {
@@ -907,17 +935,23 @@ extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
         if (fresh) {
             member_load(m, a, i, c);
             o.init(m.t, m.x, m.dx, m.aux, a.op);
+#if defined(CLODE_OBS_SPLIT)
+            fs.init(m.t);
+#endif
             step = 0;
             records = 0;
             t1 = member_t1(a, i);
             fresh = tail = hmin_fail = false;
             first = true;
-            complete = recording;
         }
         bool running = i >= 0;
         for (int k = 0; k < CLODE_STEP_BLOCK; ++k) {
             if (!__any_sync(0xffffffffu, running))
                 break;
+            if (row >= R) {
+                full = true;
+                break;
+            }
             bool valid = false;
             if (running) {
                 // the warm-up pass runs while t < t1; the feature pass while
@@ -940,14 +974,16 @@ extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
                     }
                 }
             }
-            if (recording && row >= R)
-                recording = false;
-            if (recording) {
+            {
                 const unsigned int vmask = __ballot_sync(0xffffffffu, valid);
                 const unsigned int smask = __ballot_sync(0xffffffffu, valid && first);
                 const unsigned long long cell = warp * R + row;
                 if (valid) {
                     realtype *r = a.rec + cell * (CLODE_REC_FIELDS * 32ull) + lane;
+#if defined(CLODE_OBS_SPLIT)
+                    Observer::rec_store(r, m.t, m.x, m.dx, m.aux, a.op);
+                    fs.update(m.t, m.x, m.dx, m.aux);
+#else
                     r[0] = m.t;
 #pragma unroll
                     for (int j = 0; j < N_VAR; ++j)
@@ -958,6 +994,7 @@ extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
 #pragma unroll
                     for (int j = 0; j < N_AUX; ++j)
                         r[(1 + 2 * N_VAR + j) * 32] = m.aux[j];
+#endif
                     ++records;
                     if (first) {
                         a.rec_member[warp * a.rec_members + starts + __popc(smask & ((1u << lane) - 1u))] = i;
@@ -970,14 +1007,12 @@ extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
                 }
                 starts += __popc(smask);
                 ++row;
-            } else if (valid) {
-                complete = false;  // a step the region had no room for
             }
         }
         if (i >= 0 && !running) {
             // the finish block is written for every member, so that the replay
             // never reads one left by an earlier run
-            const bool replayable = complete && records > 0;
+            const bool replayable = records > 0;
             Finish f;
             f.t = m.t;
             f.dt = m.dt;
@@ -990,6 +1025,9 @@ extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
             f.records = records;
             f.flags = replayable ? (FIN_COMPLETE | (hmin_fail ? FIN_HMIN_FAIL : 0)) : 0u;
             f.pad = 0;
+#if defined(CLODE_OBS_SPLIT)
+            f.fs = fs;
+#endif
             fin_store(f, a, i);
             if (!replayable)
                 fallback_push(a, i);
@@ -1002,6 +1040,17 @@ extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
             o.arm(m.t, m.x, m.dx, m.aux, a.op);
             park_store(o, a, i);
             i = -1;
+        }
+        if (full) {
+            // the members still running are run again by the plain passes;
+            // their finish blocks say so, for the rows they did record
+            if (i >= 0) {
+                Finish f = {};
+                fin_store(f, a, i);
+                rewarm_push(a, i);
+                i = -1;
+            }
+            break;
         }
     }
     if (lane == 0)
@@ -1016,17 +1065,21 @@ __device__ __forceinline__ void prefetch_l2(const void *p, unsigned int bytes)
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// rows ahead of the replay that are prefetched into L2, in blocks of this many rows
+// rows ahead of the replay that are prefetched into L2, in blocks of this
+// many rows (the path without shared-memory stages)
 #ifndef CLODE_REPLAY_AHEAD
 #define CLODE_REPLAY_AHEAD 8
 #endif
 #define CLODE_REPLAY_PF_ROWS 4
 
-// The replay kernel is bound by memory latency and the observer's work, not
-// by occupancy alone: its own register cap keeps the observer state in
-// registers (no local-memory spills).
+// The replay launch has the recording launch's grid (a warp per region), so
+// its blocks must fit on an SM as many at a time as the recording launch's:
+// with a program register cap (CLODE_MAXNREG) the replay takes the same cap;
+// without one, a cap that keeps the observer state in registers.
 #ifndef CLODE_REPLAY_MAXNREG
-#if defined(CLODE_DOUBLE_PRECISION)
+#if defined(CLODE_MAXNREG)
+#define CLODE_REPLAY_MAXNREG CLODE_MAXNREG
+#elif defined(CLODE_DOUBLE_PRECISION)
 #define CLODE_REPLAY_MAXNREG 255
 #elif CLODE_PRECISE
 #define CLODE_REPLAY_MAXNREG 216
@@ -1035,115 +1088,320 @@ __device__ __forceinline__ void prefetch_l2(const void *p, unsigned int bytes)
 #endif
 #endif
 
+// ---- shared-memory stages of the replay (TMA bulk copies, mbarriers) ----
+// Each warp of the replay owns a ring of rec_stages row slots and two slots
+// of 16 rows' masks in dynamic shared memory, each slot with an mbarrier
+// that counts the bytes of its copy.  Lane 0 issues one bulk copy
+// (cp.async.bulk, global -> shared) per row and one per 16 rows of masks;
+// all lanes wait on the slot's barrier, read their column and, once the
+// warp has read the slot, lane 0 refills it with the row rec_stages ahead.
+// Every wait is bounded: after CLODE_STAGE_WAIT_NS the warp records the
+// failure in *rec_error, waits (bounded again) for its copies in flight and
+// stops.
+#ifndef CLODE_STAGE_WAIT_NS
+#define CLODE_STAGE_WAIT_NS 2000000000ull
+#endif
+
+// bytes of one warp's stages: rows, two mask slots, the barriers
+__device__ __forceinline__ unsigned int stage_bytes(unsigned int stages, unsigned int row_bytes)
+{
+    return (stages * row_bytes + 256u + 8u * (stages + 2u) + 15u) & ~15u;
+}
+
+__device__ __forceinline__ unsigned int smem_addr(const void *p)
+{
+    unsigned long long s;
+    asm("cvta.to.shared.u64 %0, %1;" : "=l"(s) : "l"(p));
+    return (unsigned int)s;
+}
+
+__device__ __forceinline__ void bar_init(unsigned int bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+
+// one bulk copy of `bytes` (a multiple of 16; both addresses 16-byte
+// aligned) into shared memory, completing on `bar`
+__device__ __forceinline__ void bulk_to_smem(unsigned int dst, const void *src, unsigned int bytes, unsigned int bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool bar_test(unsigned int bar, unsigned int parity)
+{
+    unsigned int done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0u;
+}
+
+// wait for the phase of `parity` of `bar`; false after CLODE_STAGE_WAIT_NS
+__device__ __forceinline__ bool bar_wait(unsigned int bar, unsigned int parity)
+{
+    if (bar_test(bar, parity))
+        return true;
+    const unsigned long long t0 = globaltimer_ns();
+    for (;;) {
+        if (bar_test(bar, parity))
+            return true;
+        if (globaltimer_ns() - t0 > CLODE_STAGE_WAIT_NS)
+            return false;
+    }
+}
+
+// The observer's feature-pass hooks for one row of a region, for this lane
+// (the replay's per-row step, from whichever copy of the row it read).
+struct ReplayLane {
+    int i;
+    unsigned int left, events, starts;
+    Observer o;
+};
+
+__device__ __forceinline__ void replay_row(ReplayLane &L, const Args &a, unsigned long long warp, unsigned int lane,
+                                           unsigned int vmask, unsigned int smask, realtype t,
+                                           const realtype (&x)[N_VAR], const realtype (&dx)[N_VAR],
+                                           const realtype (&aux)[NA1], Counters &c)
+{
+    const unsigned long long n = (unsigned long long)a.nPts;
+    if ((smask >> lane) & 1u) {
+        const int j = a.rec_member[warp * a.rec_members + L.starts + __popc(smask & ((1u << lane) - 1u))];
+        const Finish *fj = reinterpret_cast<const Finish *>(a.fin + (unsigned long long)j * CLODE_FIN_STRIDE);
+        L.i = -1;
+        if (fj->flags & FIN_COMPLETE) {
+            L.i = j;
+            L.left = fj->records;
+            L.events = 0;
+            park_load(L.o, a, L.i);
+        }
+    }
+    L.starts += __popc(smask);
+    if (L.i < 0 || !((vmask >> lane) & 1u))
+        return;
+    const int i = L.i;
+#if defined(CLODE_OBS_SPLIT)
+    L.o.update_split(t, x, dx, aux, a.op);
+#else
+    L.o.update(t, x, dx, aux, a.op);
+#endif
+    if (L.o.event(t, x, dx, aux, a.op)) {
+        ++L.events;
+        if (L.o.on_event(t, x, dx, aux, a.op)) {
+            fallback_push(a, i);
+            L.i = -1;
+            return;
+        }
+    }
+    if (--L.left == 0) {
+        Finish f;
+        fin_load(f, a, i);
+#if defined(CLODE_OBS_SPLIT)
+        {
+            Observer armed;  // still parked: the replay stores the state only below
+            park_load(armed, a, i);
+            L.o.merge(armed, f.fs);
+        }
+#endif
+        FOut out = {a.F, n, i, 0};
+        L.o.write(out);
+        L.o.rebase(f.t - member_t0(a, i));
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            a.xf[j * n + i] = f.x[j];
+#if CLODE_STOCHASTIC
+        a.rng[i] = f.s0;
+        a.rng[n + i] = f.s1;
+#endif
+        a.dt[i] = f.dt;
+        a.tf[i] = f.t;
+        park_store(L.o, a, i);
+        if (a.status)
+            a.status[i] = status_bits(f.t, f.x, f.steps, a, member_t1(a, i), (f.flags & FIN_HMIN_FAIL) != 0, false);
+        c.events += L.events;
+        L.i = -1;
+    }
+}
+
+// this lane's column of a row (fields of 32 lanes each, from global or shared memory)
+__device__ __forceinline__ void column_load(const realtype *r, realtype &t, realtype (&x)[N_VAR],
+                                            realtype (&dx)[N_VAR], realtype (&aux)[NA1], const ObserverParams &op)
+{
+#if defined(CLODE_OBS_SPLIT)
+    Observer::rec_load(r, t, x, dx, aux, op);
+#else
+    t = r[0];
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j)
+        x[j] = r[(1 + j) * 32];
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j)
+        dx[j] = r[(1 + N_VAR + j) * 32];
+#pragma unroll
+    for (int j = 0; j < NA1; ++j)
+        aux[j] = j < N_AUX ? r[(1 + 2 * N_VAR + j) * 32] : ZERO;
+#endif
+}
+
 // Feature pass by replay: one warp per region of the recording launch (the
 // same grid), each lane walking its column.  A member starts where its lane
 // recorded its first step, with the observer state parked (armed) by the
 // recording launch; it ends at its last stored step with the feature pass's
 // final state from its finish block.  A member whose observer ends it early
 // (its event limit) goes to the fallback list, since the state at that step
-// was not stored whole.  The rows a few steps ahead are prefetched into L2.
-extern "C" __global__ void __maxnreg__(CLODE_REPLAY_MAXNREG) clode_features_replay(const Args a)
+// was not stored whole.  clode_features_replay_staged takes the rows
+// through the warp's rec_stages (>= 2) shared-memory stages (dynamic shared
+// memory of blockDim.x / 32 times stage_bytes); clode_features_replay
+// reads them from global memory, the rows a few steps ahead prefetched
+// into L2.
+template <bool STAGED>
+__device__ __forceinline__ void features_replay(const Args &a)
 {
+    extern __shared__ __align__(128) unsigned char replay_smem[];
     Counters c = {0, 0, 0, 0};
     const unsigned int lane = threadIdx.x & 31u;
     const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long R = a.rec_rows;
     const unsigned long long rows = a.rec_used[warp];
-    const unsigned long long n = (unsigned long long)a.nPts;
     const unsigned int row_bytes = CLODE_REC_FIELDS * 32u * (unsigned int)sizeof(realtype);
-    unsigned int starts = 0;
-    int i = -1;
-    unsigned int left = 0, events = 0;
-    Observer o;
-    // the first rows of the region into L2 (R is a multiple of 16, so every
-    // region's masks start on a 16-byte boundary)
-    if (lane == 0) {
-        const unsigned long long first = rows < CLODE_REPLAY_AHEAD ? rows : CLODE_REPLAY_AHEAD;
-        if (first > 0) {
-            prefetch_l2(a.rec + warp * R * (CLODE_REC_FIELDS * 32ull), (unsigned int)first * row_bytes);
-            prefetch_l2(a.rec_mask + 2 * warp * R, (unsigned int)((first * 8 + 15) / 16 * 16));
+    const unsigned int S = a.rec_stages;
+    ReplayLane L;
+    L.i = -1;
+    L.left = L.events = L.starts = 0;
+    realtype t, x[N_VAR], dx[N_VAR], aux[NA1];
+    if (STAGED) {
+        unsigned char *base = replay_smem + (threadIdx.x >> 5) * stage_bytes(S, row_bytes);
+        const unsigned int s_rows = smem_addr(base);
+        const unsigned int s_masks = s_rows + S * row_bytes;
+        const unsigned int s_bars = s_masks + 256u;  // S row barriers, then 2 mask barriers
+        const unsigned int *masks = reinterpret_cast<const unsigned int *>(base + S * row_bytes);
+        const realtype *region = a.rec + warp * R * (CLODE_REC_FIELDS * 32ull);
+        const unsigned int *region_masks = a.rec_mask + 2 * warp * R;
+        // rows [0, issued) and mask chunks [0, chunks_issued) have been requested
+        unsigned long long issued = 0, chunks_issued = 0;
+        const unsigned long long chunks = (rows + 15) / 16;
+        if (lane == 0 && rows > 0) {
+            for (unsigned int k = 0; k < S + 2; ++k)
+                bar_init(s_bars + 8u * k);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
-    }
-    for (unsigned long long row = 0; row < rows; ++row) {
-        const unsigned long long cell = warp * R + row;
-        // keep CLODE_REPLAY_AHEAD rows in flight: every CLODE_REPLAY_PF_ROWS rows,
-        // the block that far ahead (within the rows recorded)
-        if (lane == 0 && row % CLODE_REPLAY_PF_ROWS == 0) {
-            const unsigned long long ahead = row + CLODE_REPLAY_AHEAD;
-            if (ahead < rows) {
-                const unsigned long long cnt =
-                    rows - ahead < CLODE_REPLAY_PF_ROWS ? rows - ahead : CLODE_REPLAY_PF_ROWS;
-                prefetch_l2(a.rec + (cell + CLODE_REPLAY_AHEAD) * (CLODE_REC_FIELDS * 32ull),
-                            (unsigned int)cnt * row_bytes);
-                // the masks: 8 bytes per row, rounded to whole 16-byte pieces
-                const unsigned long long b0 = (2 * (cell + CLODE_REPLAY_AHEAD) * 4) & ~15ull;
-                const unsigned long long b1 = (2 * (cell + CLODE_REPLAY_AHEAD + cnt) * 4 + 15) & ~15ull;
-                prefetch_l2(reinterpret_cast<const char *>(a.rec_mask) + b0, (unsigned int)(b1 - b0));
+        __syncwarp();
+        if (rows > 0) {
+            if (lane == 0) {
+                for (; issued < rows && issued < S; ++issued)
+                    bulk_to_smem(s_rows + (unsigned int)issued * row_bytes, region + issued * (CLODE_REC_FIELDS * 32ull),
+                                 row_bytes, s_bars + 8u * (unsigned int)issued);
+                for (; chunks_issued < chunks && chunks_issued < 2; ++chunks_issued)
+                    bulk_to_smem(s_masks + 128u * (unsigned int)chunks_issued, region_masks + 32 * chunks_issued, 128u,
+                                 s_bars + 8u * (S + (unsigned int)chunks_issued));
+            }
+            issued = rows < S ? rows : S;
+            chunks_issued = chunks < 2 ? chunks : 2;
+        }
+        // a lane that saw a stage not filled in time processes no more rows;
+        // the warp checks for that once per 16 rows and leaves together
+        bool ok = true;
+        unsigned int slot = 0, phase = 0;  // row % S, (row / S) & 1
+        unsigned long long row = 0;
+        for (; row < rows; ++row) {
+            const unsigned long long chunk = row >> 4;
+            if ((row & 15) == 0) {
+                if (__any_sync(0xffffffffu, !ok))
+                    break;
+                ok = bar_wait(s_bars + 8u * (S + (unsigned int)(chunk & 1)), (unsigned int)(chunk >> 1) & 1u);
+            }
+            if (ok)
+                ok = bar_wait(s_bars + 8u * slot, phase);
+            const unsigned int *mk = masks + 32u * (unsigned int)(chunk & 1) + 2u * (unsigned int)(row & 15);
+            const unsigned int vmask = mk[0], smask = mk[1];
+            column_load(reinterpret_cast<const realtype *>(base + slot * row_bytes) + lane, t, x, dx, aux, a.op);
+            // the warp has read the slot (and, at a chunk's last row, the
+            // chunk's masks): refill them
+            __syncwarp();
+            if (lane == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                if (issued < rows)
+                    bulk_to_smem(s_rows + slot * row_bytes, region + issued * (CLODE_REC_FIELDS * 32ull), row_bytes,
+                                 s_bars + 8u * slot);
+                if ((row & 15) == 15 && chunks_issued < chunks) {
+                    const unsigned int ms = (unsigned int)(chunks_issued & 1);
+                    bulk_to_smem(s_masks + 128u * ms, region_masks + 32 * chunks_issued, 128u, s_bars + 8u * (S + ms));
+                }
+            }
+            if (issued < rows)
+                ++issued;
+            if ((row & 15) == 15 && chunks_issued < chunks)
+                ++chunks_issued;
+            if (++slot == S) {
+                slot = 0;
+                phase ^= 1u;
+            }
+            if (ok)
+                replay_row(L, a, warp, lane, vmask, smask, t, x, dx, aux, c);
+        }
+        if (__any_sync(0xffffffffu, !ok)) {
+            // a stage that was not filled in time: record it, and wait (bounded)
+            // for every copy this warp still has in flight before leaving
+            if (lane == 0) {
+                atomicOr(a.rec_error, 1u);
+                for (unsigned long long r = row; r < issued; ++r)
+                    bar_wait(s_bars + 8u * (unsigned int)(r % S), (unsigned int)(r / S) & 1u);
+                for (unsigned long long k = row >> 4; k < chunks_issued; ++k)
+                    bar_wait(s_bars + 8u * (S + (unsigned int)(k & 1)), (unsigned int)(k >> 1) & 1u);
+            }
+            __syncwarp();
+        }
+    } else {
+        // the first rows of the region into L2 (R is a multiple of 16, so every
+        // region's masks start on a 16-byte boundary)
+        if (lane == 0) {
+            const unsigned long long first = rows < CLODE_REPLAY_AHEAD ? rows : CLODE_REPLAY_AHEAD;
+            if (first > 0) {
+                prefetch_l2(a.rec + warp * R * (CLODE_REC_FIELDS * 32ull), (unsigned int)first * row_bytes);
+                prefetch_l2(a.rec_mask + 2 * warp * R, (unsigned int)((first * 8 + 15) / 16 * 16));
             }
         }
-        // the row's masks and this lane's column are loaded together, before
-        // anything depends on them, so a row costs one memory latency (a
-        // hole in the column is loaded too, and ignored)
-        const unsigned int vmask = a.rec_mask[2 * cell];
-        const unsigned int smask = a.rec_mask[2 * cell + 1];
-        const realtype *r = a.rec + cell * (CLODE_REC_FIELDS * 32ull) + lane;
-        const realtype t = r[0];
-        realtype x[N_VAR], dx[N_VAR], aux[NA1];
-#pragma unroll
-        for (int j = 0; j < N_VAR; ++j)
-            x[j] = r[(1 + j) * 32];
-#pragma unroll
-        for (int j = 0; j < N_VAR; ++j)
-            dx[j] = r[(1 + N_VAR + j) * 32];
-#pragma unroll
-        for (int j = 0; j < NA1; ++j)
-            aux[j] = j < N_AUX ? r[(1 + 2 * N_VAR + j) * 32] : ZERO;
-        if ((smask >> lane) & 1u) {
-            const int j = a.rec_member[warp * a.rec_members + starts + __popc(smask & ((1u << lane) - 1u))];
-            const Finish *fj = reinterpret_cast<const Finish *>(a.fin + (unsigned long long)j * CLODE_FIN_STRIDE);
-            i = -1;
-            if (fj->flags & FIN_COMPLETE) {
-                i = j;
-                left = fj->records;
-                events = 0;
-                park_load(o, a, i);
+        for (unsigned long long row = 0; row < rows; ++row) {
+            const unsigned long long cell = warp * R + row;
+            // keep CLODE_REPLAY_AHEAD rows in flight: every CLODE_REPLAY_PF_ROWS rows,
+            // the block that far ahead (within the rows recorded)
+            if (lane == 0 && row % CLODE_REPLAY_PF_ROWS == 0) {
+                const unsigned long long ahead = row + CLODE_REPLAY_AHEAD;
+                if (ahead < rows) {
+                    const unsigned long long cnt =
+                        rows - ahead < CLODE_REPLAY_PF_ROWS ? rows - ahead : CLODE_REPLAY_PF_ROWS;
+                    prefetch_l2(a.rec + (cell + CLODE_REPLAY_AHEAD) * (CLODE_REC_FIELDS * 32ull),
+                                (unsigned int)cnt * row_bytes);
+                    // the masks: 8 bytes per row, rounded to whole 16-byte pieces
+                    const unsigned long long b0 = (2 * (cell + CLODE_REPLAY_AHEAD) * 4) & ~15ull;
+                    const unsigned long long b1 = (2 * (cell + CLODE_REPLAY_AHEAD + cnt) * 4 + 15) & ~15ull;
+                    prefetch_l2(reinterpret_cast<const char *>(a.rec_mask) + b0, (unsigned int)(b1 - b0));
+                }
             }
-        }
-        starts += __popc(smask);
-        if (i < 0 || !((vmask >> lane) & 1u))
-            continue;
-        o.update(t, x, dx, aux, a.op);
-        if (o.event(t, x, dx, aux, a.op)) {
-            ++events;
-            if (o.on_event(t, x, dx, aux, a.op)) {
-                fallback_push(a, i);
-                i = -1;
-                continue;
-            }
-        }
-        if (--left == 0) {
-            Finish f;
-            fin_load(f, a, i);
-            FOut out = {a.F, n, i, 0};
-            o.write(out);
-            o.rebase(f.t - member_t0(a, i));
-#pragma unroll
-            for (int j = 0; j < N_VAR; ++j)
-                a.xf[j * n + i] = f.x[j];
-#if CLODE_STOCHASTIC
-            a.rng[i] = f.s0;
-            a.rng[n + i] = f.s1;
-#endif
-            a.dt[i] = f.dt;
-            a.tf[i] = f.t;
-            park_store(o, a, i);
-            if (a.status)
-                a.status[i] = status_bits(f.t, f.x, f.steps, a, member_t1(a, i), (f.flags & FIN_HMIN_FAIL) != 0, false);
-            c.events += events;
-            i = -1;
+            // the row's masks and this lane's column are loaded together, before
+            // anything depends on them, so a row costs one memory latency (a
+            // hole in the column is loaded too, and ignored)
+            const unsigned int vmask = a.rec_mask[2 * cell];
+            const unsigned int smask = a.rec_mask[2 * cell + 1];
+            column_load(a.rec + cell * (CLODE_REC_FIELDS * 32ull) + lane, t, x, dx, aux, a.op);
+            replay_row(L, a, warp, lane, vmask, smask, t, x, dx, aux, c);
         }
     }
     flush_counters(a, c);
+}
+
+extern "C" __global__ void __maxnreg__(CLODE_REPLAY_MAXNREG) clode_features_replay(const Args a)
+{
+    features_replay<false>(a);
+}
+
+extern "C" __global__ void __maxnreg__(CLODE_REPLAY_MAXNREG) clode_features_replay_staged(const Args a)
+{
+    features_replay<true>(a);
 }
 #endif  // !CLODE_FEATURE_STORE
 #endif  // CLODE_HAVE_OBSERVER

