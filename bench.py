@@ -49,11 +49,13 @@ FLOPS_PER_STEP_OBS = 5 * N_VAR + 3 * N_AUX + 6  # nhood2 per-step extrema and me
 # build on the 512 x 512 case (262,144 members: 76.6 MB + 519.6 MB), scaled
 # by members; the traffic is per-member state, so it grows in proportion
 DRAM_BYTES_PER_MEMBER = (36643072 + 39959552 + 216447488 + 303181824) / 262144
-# the replayed feature pass: bytes of one stored step (t, x, dx, aux in FP32)
-REC_BYTES = (1 + 2 * N_VAR + N_AUX) * 4
-# DRAM bytes (read + write) per member of the recording warm-up launches of a
-# replayed map (ncu, 512 x 512 case, scaled by members; see profiles/)
-REC_DRAM_BYTES_PER_MEMBER = None
+# DRAM bytes (read + write) per recorded step of the recording and of the
+# replay launches of a replayed map: ncu dram__bytes_{read,write}.sum of all
+# six launches of each kind (three maps of two launch pairs) of the default
+# build on the 512 x 512 case, divided by the three maps' steps (3 x
+# 1,463,676,130); the traffic is the stored rows, so it grows with the steps
+REC_DRAM_BYTES_PER_STEP = (10699342336 + 110497920768) / (3 * 1463676130)
+REPLAY_DRAM_BYTES_PER_STEP = (113871344384 + 1407749888) / (3 * 1463676130)
 
 
 def measured_hbm_peak() -> tuple[float, str]:
@@ -171,7 +173,11 @@ def run_cpu(x0, pars, tspan, idx, nthreads: int, prefer_reference: bool = True, 
     return s.get_F(), secs, ("reference" if use_ref else "port")
 
 
-SURROGATE_FEATURES = ("mean v", "max v", "min v", "mean c")
+# screened feature sets: the extent of v and c (continuous over the map),
+# and the same with nhood2's event and spike counts and mean period, which
+# jump where the number of spikes per burst or the oscillation changes
+SURROGATE_FEATURES = ("mean v", "max v", "min v", "mean c", "event count", "max peaks", "mean peaks", "mean period")
+SURROGATE_SETS = {"counts": SURROGATE_FEATURES, "extent": SURROGATE_FEATURES[:4]}
 
 
 def bench_surrogate(args, tuned_options: dict) -> dict:
@@ -179,14 +185,17 @@ def bench_surrogate(args, tuned_options: dict) -> dict:
 
     Map: lactotroph, G2 x G2 grid of (gcal, gbk) (default 4096 x 4096), fixed
     tspan [0, 3000] ms (the surrogate learns a function of the two parameters),
-    DP45 rtol 1e-6 FP32, nhood2; features mean v, max v, min v, mean c.
-    Plain: every point integrated by the engine.  Screened: a 513 x 513
-    sub-grid integrated, the network trained on it on the GPU, the full grid
-    predicted, 65,536 random interior points integrated to calibrate the
-    cell screen, every point of a rejected cell integrated again.  Error of a
-    point: max over the features of |screened - plain| / (the feature's range
-    over the plain map), reported over the whole map and over 65,536 seeded
-    held-out points.
+    DP45 rtol 1e-6 FP32, nhood2.  Two screens of the same plain map: the
+    eight features of SURROGATE_FEATURES (extent of v and c, event count,
+    max and mean spikes per event, mean period) and the first four alone.
+    Plain: every point integrated by the engine (timed once, all eight
+    features).  Screened: a 513 x 513 sub-grid integrated, the network
+    trained on it on the GPU, the full grid predicted, 65,536 random interior
+    points integrated to calibrate the cell screen, every point of a rejected
+    cell integrated again.  Error of a point: max over the screen's features
+    of |screened - plain| / (the feature's range over the plain map),
+    reported over the whole map, over 65,536 seeded held-out points, and per
+    feature.
     """
     from clode_gb300 import clode_cpp_wrapper as W, rhs_path
     from clode_gb300.surrogate import FeatureMapScreen
@@ -218,33 +227,45 @@ def bench_surrogate(args, tuned_options: dict) -> dict:
     P0, P1 = P0.ravel(), P1.ravel()
     integrate(P0[:4096], P1[:4096])  # build and warm-up
     t0 = time.perf_counter()
-    plain = integrate(P0, P1)
+    plain_all = integrate(P0, P1)
     t_plain = time.perf_counter() - t0
-    scr = FeatureMapScreen(integrate, lo=(0.5, 0.0), hi=(3.0, 2.0), n_features=len(SURROGATE_FEATURES), seed=1)
     stride = args.surrogate_stride if args.surrogate_stride > 0 else max(G // 512, 1)
-    res = scr.run(G, G, train_stride=stride, steps=args.surrogate_steps, batch=args.surrogate_batch,
-                  tol=0.01, keep=0.99, n_calibration=65536, refine=bool(args.surrogate_refine))
-    scale = plain.max(axis=0) - plain.min(axis=0)
-    err = FeatureMapScreen.map_error(res.features, plain, scale)
     rng = np.random.default_rng(args.seed ^ 0xC0DE)
     held = rng.choice(G * G, size=min(65536, G * G), replace=False)
-    return {
-        "workload": f"lactotroph nhood2 map {G}x{G}, tspan [0,3000] ms, features {list(SURROGATE_FEATURES)}",
-        "training": {"steps": args.surrogate_steps, "batch": args.surrogate_batch, "stride": stride,
-                     "refine": bool(args.surrogate_refine)},
-        "error_measure": "max over features of |screened - plain| / feature range over the plain map",
-        "points": G * G, "plain_points_per_s": G * G / t_plain, "screened_points_per_s": res.timings["points_per_s"],
-        "speedup_vs_plain": t_plain / res.timings["total_s"], "integrated_fraction": res.integrated_fraction,
-        "fallback_fraction": res.fallback_fraction,
-        "map": {"within_1pct": float(np.mean(err <= 0.01)), "err_median": float(np.median(err)),
-                "err_p99": float(np.quantile(err, 0.99)), "err_max": float(err.max())},
-        "heldout": {"points": int(held.size), "within_1pct": float(np.mean(err[held] <= 0.01)),
-                    "err_median": float(np.median(err[held])), "err_p99": float(np.quantile(err[held], 0.99))},
-        "final_loss": float(res.loss[-20:].mean()) if res.loss is not None and res.loss.size else None,
-        "timings_s": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.timings.items()
-                      if k != "feature_scale"},
-        "plain_s": t_plain,
-    }
+    out = {"workload": f"lactotroph nhood2 map {G}x{G}, tspan [0,3000] ms",
+           "training": {"steps": args.surrogate_steps, "batch": args.surrogate_batch, "stride": stride,
+                        "refine": bool(args.surrogate_refine)},
+           "error_measure": "max over the screen's features of |screened - plain| / feature range over the plain map",
+           "points": G * G, "plain_points_per_s": G * G / t_plain, "plain_s": t_plain}
+    for key, feats in SURROGATE_SETS.items():
+        sel = [SURROGATE_FEATURES.index(f) for f in feats]
+        plain = plain_all[:, sel]
+        scr = FeatureMapScreen(lambda a, b: integrate(a, b)[:, sel], lo=(0.5, 0.0), hi=(3.0, 2.0),
+                               n_features=len(feats), seed=1)
+        res = scr.run(G, G, train_stride=stride, steps=args.surrogate_steps, batch=args.surrogate_batch,
+                      tol=0.01, keep=0.99, n_calibration=65536, refine=bool(args.surrogate_refine))
+        scale = plain.max(axis=0) - plain.min(axis=0)
+        err = FeatureMapScreen.map_error(res.features, plain, scale)
+        per_feature = np.abs(np.asarray(res.features, np.float64) - plain) / np.maximum(scale, 1e-30)
+        out[key] = {
+            "features": list(feats),
+            "screened_points_per_s": res.timings["points_per_s"],
+            "speedup_vs_plain": t_plain / res.timings["total_s"], "integrated_fraction": res.integrated_fraction,
+            "fallback_fraction": res.fallback_fraction,
+            "map": {"within_1pct": float(np.mean(err <= 0.01)), "err_median": float(np.median(err)),
+                    "err_p99": float(np.quantile(err, 0.99)), "err_max": float(err.max())},
+            "heldout": {"points": int(held.size), "within_1pct": float(np.mean(err[held] <= 0.01)),
+                        "err_median": float(np.median(err[held])), "err_p99": float(np.quantile(err[held], 0.99))},
+            "within_1pct_per_feature": {f: float(np.mean(per_feature[:, j] <= 0.01)) for j, f in enumerate(feats)},
+            "final_loss": float(res.loss[-20:].mean()) if res.loss is not None and res.loss.size else None,
+            "timings_s": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.timings.items()
+                          if k != "feature_scale"},
+        }
+        del scr
+    # the headline screen: the one with the counts
+    out.update({k: out["counts"][k] for k in ("screened_points_per_s", "speedup_vs_plain", "fallback_fraction",
+                                              "integrated_fraction", "map", "heldout")})
+    return out
 
 
 def bench_trajectory(args, tuned_options: dict) -> dict:
@@ -651,8 +672,9 @@ def main():
             kernel_ms.append(sim.last_kernel_ms())
             stats.append(sim.get_stats())
             split.append({k: sim.get_option(k) for k in ("replay_chunks", "replay_fallback", "replay_rewarm",
-                                                          "replay_stages_used", "replay_rows", "replay_record_ms",
-                                                          "replay_replay_ms", "replay_fallback_ms", "warmup_ms")})
+                                                          "replay_stages_used", "replay_rows", "replay_row_bytes",
+                                                          "replay_record_ms", "replay_replay_ms",
+                                                          "replay_fallback_ms", "warmup_ms")})
             l2_flush()
         wall_dev = time.perf_counter() - t0
     barrier()
@@ -699,16 +721,19 @@ def main():
     rhs_per_s = st["rhs_evals"] / (ms / 1e3)
     if replayed:
         # the recording warm-up launches integrate (stages, right-hand sides,
-        # controller): FP32-bound; the replay launches read the stored steps
-        # (t, x, dx, aux: REC_BYTES per step) and run the observer: HBM-bound
+        # controller): FP32-bound; the replay launches read the stored rows
+        # (per warp-wide row: the observer's fields of 32 lanes and two masks)
+        # and run the observer: HBM-bound
         rec_ms = sp_["replay_record_ms"]
         flops = st["rhs_evals"] * FLOPS_PER_RHS + attempts * FLOPS_PER_ATTEMPT
         achieved_tflops = flops / (rec_ms / 1e3) / 1e12
-        rep_bytes = st["steps"] * REC_BYTES
+        rep_bytes = sp_["replay_rows"] * sp_["replay_row_bytes"]
         roof_replay = {"bound": "hbm", "achieved": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9,
                        "peak": hbm_peak, "unit": "GB/s",
                        "frac": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9 / hbm_peak,
-                       "traffic": None, "bytes_per_step": REC_BYTES,
+                       "traffic": REPLAY_DRAM_BYTES_PER_STEP * st["steps"] if REPLAY_DRAM_BYTES_PER_STEP else None,
+                       "algorithmic_bytes": rep_bytes, "rows": sp_["replay_rows"],
+                       "row_bytes": sp_["replay_row_bytes"],
                        "peak_source": hbm_src,
                        "kernel": "clode_features_replay_staged" if sp_["replay_stages_used"] >= 2
                        else "clode_features_replay",
@@ -745,9 +770,10 @@ def main():
         "wall_ms_per_step_device_loop": 1e3 * wall_dev / args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
                      "frac": achieved_tflops / peak_tflops,
-                     "traffic": ((REC_DRAM_BYTES_PER_MEMBER or 0) if replayed else DRAM_BYTES_PER_MEMBER) * n
-                     or None,
-                     "traffic_source": "ncu DRAM bytes of the 512 x 512 map, scaled by members",
+                     "traffic": ((REC_DRAM_BYTES_PER_STEP * st["steps"] if REC_DRAM_BYTES_PER_STEP else None)
+                                 if replayed else DRAM_BYTES_PER_MEMBER * n),
+                     "traffic_source": "ncu DRAM bytes of the 512 x 512 map, scaled by "
+                                       + ("recorded steps" if replayed else "members"),
                      "peak_source": f"nominal FP32 FMA rate {info.compute_units} SMs x 128 lanes x 2 at the "
                                     f"median sampled SM clock {sm_mhz:.0f} MHz",
                      "kernel": "clode_init_observer_record" if replayed else "clode_init_observer + clode_features",

@@ -2490,6 +2490,8 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "replay_stages_used") *value = sim->last_stages;
         else if (k == "replay_rewarm") *value = sim->last_rewarm;
         else if (k == "replay_rows") *value = sim->last_rows;
+        else if (k == "replay_row_bytes")  // one warp-wide row: every stored field of 32 lanes and the two masks
+            *value = sim->rec_fields ? (double)sim->rec_fields * 32.0 * (double)sim->real_size() + 8.0 : 0.0;
         else if (k == "warmup_ms") *value = sim->last_warmup_ms;
         else if (k == "replay_chunks") *value = sim->last_replay_chunks;
         else if (k == "replay_fallback") *value = sim->last_fallback;

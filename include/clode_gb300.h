@@ -322,7 +322,8 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * "last_block", and of the last replayed run "replay_chunks" (launch pairs),
  * "replay_fallback" (members given to the plain passes), "replay_rewarm" (of
  * those, members whose warm-up a full region cut short), "replay_rows" (rows
- * recorded), "replay_stages_used", "warmup_ms" (the separate warm-up launch
+ * recorded), "replay_row_bytes" (bytes of one warp-wide row of the built
+ * program), "replay_stages_used", "warmup_ms" (the separate warm-up launch
  * of the last integrated features run),
  * "replay_record_ms", "replay_replay_ms", "replay_fallback_ms" (device time
  * of each launch kind).
