@@ -525,10 +525,20 @@ class SimulatorBase:
         _check(N.lib.clode_sim_shift_x0(self._handle))
 
     # getters
-    def _get(self, which: int) -> np.ndarray:
+    def _get(self, which: int, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """The array `which` as float64; into `out` (a C-contiguous float64
+        array of at least that many elements, e.g. in page-locked memory that
+        a caller reuses between calls) when given, returning its leading part."""
         n = C.c_size_t(0)
         _check(N.lib.clode_sim_get(self._handle, which, None, 0, C.byref(n)))
-        out = np.empty(n.value, dtype=np.float64)
+        if out is None:
+            out = np.empty(n.value, dtype=np.float64)
+        else:
+            if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or not out.flags["WRITEABLE"]:
+                raise ValueError("out must be a writeable C-contiguous float64 array")
+            if out.size < n.value:
+                raise ValueError(f"out holds {out.size} values, {n.value} needed")
+            out = out.reshape(-1)[:n.value]
         if n.value:
             _check(N.lib.clode_sim_get(self._handle, which, N.dptr(out), out.size, C.byref(n)))
         return out
@@ -821,8 +831,11 @@ class FeatureSimulatorBase(SimulatorBase, _StoredRows):
     def get_observer_name(self) -> str:
         return self._get_string(N.STRING_OBSERVER_NAME)
 
-    def get_f(self) -> np.ndarray:
-        return self._get(N.ARRAY_F)
+    def get_f(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Features, [k * nPts + i] (clode/cpp/CLODEfeatures.hpp getF); `out`:
+        optional destination (see SimulatorBase._get; no reference
+        counterpart)."""
+        return self._get(N.ARRAY_F, out)
 
     def get_n_features(self) -> int:
         s = N.CSizes()

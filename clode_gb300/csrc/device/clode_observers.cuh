@@ -713,7 +713,7 @@ struct Observer {
         ext.update(x, dx, aux, h, t - t_start);
         update_events(op);
     }
-#if !CLODE_PRECISE
+#if !CLODE_PRECISE && !defined(CLODE_REPLAY_WHOLE_ROWS)
 #define CLODE_OBS_SPLIT 1
     // the replayed feature pass: rows of t, every state variable and the
     // slope of fVar (the centre, ball and peak tests); the extent and step
@@ -916,7 +916,7 @@ struct Observer {
         ext.update(x, dx, aux, h, t - t_start);
         update_events(t, x, dx, h, op);
     }
-#if !CLODE_PRECISE
+#if !CLODE_PRECISE && !defined(CLODE_REPLAY_WHOLE_ROWS)
 #define CLODE_OBS_SPLIT 1
     // the replayed feature pass: rows of t and the state and slope of eVar
     // and fVar; the extent and step statistics come from the recording

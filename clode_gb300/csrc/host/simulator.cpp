@@ -257,6 +257,7 @@ struct clode_sim {
     int replay_stages = 0;      // shared-memory row stages per replay warp (0: rows read from global memory;
                                 // -1: up to 4 that fit)
     double replay_cap_scale = 1.0;  // autotuner trials on a sample: the regions' memory scaled by its fraction
+    bool replay_split = true;   // rows of the observer's event fields, the pass's sums taken while recording
     unsigned int last_stages = 0;          // stages the last replayed run used
     unsigned int last_rewarm = 0;          // of last_fallback: members whose warm-up was run again
     double last_rows = 0.0;                // rows the last replayed run recorded (all regions, all launches)
@@ -471,6 +472,8 @@ struct clode_sim {
             s.defines.push_back("-DN_STORE_EVENTS=" + std::to_string(op.max_event_timestamps));
             if (want_store)
                 s.defines.push_back("-DCLODE_FEATURE_STORE=1");
+            if (!replay_split)
+                s.defines.push_back("-DCLODE_REPLAY_WHOLE_ROWS=1");
         } else {
             s.defines.push_back("-DN_STORE_EVENTS=0");
         }
@@ -2447,6 +2450,11 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 sim->rec_mask.release();
                 sim->rec_member.release();
             }
+        } else if (k == "replay_split") {
+            if ((value != 0.0) != sim->replay_split) {
+                sim->replay_split = value != 0.0;
+                sim->built = false;
+            }
         } else if (k == "replay_stages") {
             if (value < -1.0 || value > 16.0)
                 fail(CLODE_ERR_INVALID_ARGUMENT, "replay_stages must be -1 (automatic) or 0 .. 16");
@@ -2487,6 +2495,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "replay") *value = sim->replay;
         else if (k == "replay_mb") *value = sim->replay_mb;
         else if (k == "replay_stages") *value = sim->replay_stages;
+        else if (k == "replay_split") *value = sim->replay_split;
         else if (k == "replay_stages_used") *value = sim->last_stages;
         else if (k == "replay_rewarm") *value = sim->last_rewarm;
         else if (k == "replay_rows") *value = sim->last_rows;
