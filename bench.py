@@ -568,6 +568,11 @@ def main():
                     help="feature pass replays the warm-up's stored steps (engine default 1)")
     ap.add_argument("--replay-mb", type=float, default=None, help="record regions in MiB (engine default: automatic)")
     ap.add_argument("--precise", type=int, default=None, help="the engine's precision option (engine default 0)")
+    ap.add_argument("--replay-split", type=int, default=None,
+                    help="replay rows of the observer's event fields with the pass's sums taken while recording "
+                         "(1, the engine default) or whole rows (0)")
+    ap.add_argument("--replay-fused", type=int, default=None,
+                    help="recording and replay in one launch per launch pair (1) or two launches (0)")
     ap.add_argument("--replay-stages", type=int, default=None,
                     help="shared-memory row stages of the replay (-1 automatic, the engine default; 0: rows read "
                          "from global memory)")
@@ -629,7 +634,8 @@ def main():
                      ("fuse_init", args.fuse_init), ("step_block", args.step_block),
                      ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm),
                      ("order_by_span", args.order_by_span), ("replay", args.replay), ("replay_mb", args.replay_mb),
-                     ("precise", args.precise), ("replay_stages", args.replay_stages)):
+                     ("precise", args.precise), ("replay_stages", args.replay_stages),
+                     ("replay_split", args.replay_split), ("replay_fused", args.replay_fused)):
         if val is not None:
             sim.set_option(key, val)
     sim.build_cl()
@@ -672,7 +678,9 @@ def main():
             kernel_ms.append(sim.last_kernel_ms())
             stats.append(sim.get_stats())
             split.append({k: sim.get_option(k) for k in ("replay_chunks", "replay_fallback", "replay_rewarm",
-                                                          "replay_stages_used", "replay_rows", "replay_row_bytes",
+                                                          "replay_stages_used", "replay_regions_per_warp",
+                                                          "replay_fused", "replay_split",
+                                                          "replay_rows", "replay_row_bytes",
                                                           "replay_record_ms", "replay_replay_ms",
                                                           "replay_fallback_ms", "warmup_ms")})
             l2_flush()
@@ -739,7 +747,7 @@ def main():
         flops = st["rhs_evals"] * FLOPS_PER_RHS + attempts * FLOPS_PER_ATTEMPT
         achieved_tflops = flops / (rec_ms / 1e3) / 1e12
         rep_bytes = sp_["replay_rows"] * sp_["replay_row_bytes"]
-        roof_replay = {"bound": "hbm", "achieved": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9,
+        roof_replay = None if sp_["replay_fused"] else {"bound": "hbm", "achieved": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9,
                        "peak": hbm_peak, "unit": "GB/s",
                        "frac": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9 / hbm_peak,
                        "traffic": REPLAY_DRAM_BYTES_PER_STEP * st["steps"] if REPLAY_DRAM_BYTES_PER_STEP else None,
@@ -781,13 +789,15 @@ def main():
         "wall_ms_per_step_device_loop": 1e3 * wall_dev / args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
                      "frac": achieved_tflops / peak_tflops,
-                     "traffic": ((REC_DRAM_BYTES_PER_STEP * st["steps"] if REC_DRAM_BYTES_PER_STEP else None)
+                     "traffic": (((REC_DRAM_BYTES_PER_STEP + (REPLAY_DRAM_BYTES_PER_STEP if sp_["replay_fused"] else 0))
+                                  * st["steps"] if REC_DRAM_BYTES_PER_STEP else None)
                                  if replayed else DRAM_BYTES_PER_MEMBER * n),
                      "traffic_source": "ncu DRAM bytes of the 512 x 512 map, scaled by "
                                        + ("recorded steps" if replayed else "members"),
                      "peak_source": f"nominal FP32 FMA rate {info.compute_units} SMs x 128 lanes x 2 at the "
                                     f"median sampled SM clock {sm_mhz:.0f} MHz",
-                     "kernel": "clode_init_observer_record" if replayed else "clode_init_observer + clode_features",
+                     "kernel": ("clode_features_record_replay" if sp_["replay_fused"] else "clode_init_observer_record")
+                     if replayed else "clode_init_observer + clode_features",
                      "ms": rec_ms, "flops_per_launch": flops},
         "roofline_replay": roof_replay,
         "replay": sp_,

@@ -127,6 +127,9 @@ struct ArgsT {
     // sets when a stage was not filled within its wait limit
     unsigned int rec_stages;
     unsigned int *rec_error;
+    // regions each replay warp takes in turn (the replay's blocks are the
+    // recording launch's, with this many times fewer threads)
+    unsigned int rec_regions_per_warp;
     SolverParamsT<R> sp;
     ObserverParamsT<R> op;
 };

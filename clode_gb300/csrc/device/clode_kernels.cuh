@@ -898,7 +898,7 @@ __device__ __forceinline__ void rewarm_push(const Args &a, int i)
 // no launch waits on a member far longer than its region.  A member that
 // takes no step goes to the fallback list and the plain feature pass runs it
 // from the parked observer state.
-extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
+__device__ __forceinline__ void record_body(const Args &a)
 {
     Counters c = {0, 0, 0, 0};
     const unsigned int lane = threadIdx.x & 31u;
@@ -1058,6 +1058,11 @@ extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
     flush_counters(a, c);
 }
 
+extern "C" __global__ void CLODE_CAP clode_init_observer_record(const Args a)
+{
+    record_body(a);
+}
+
 // L2 prefetch of a contiguous global range (TMA bulk prefetch; 16-byte
 // aligned start, size a multiple of 16 bytes)
 __device__ __forceinline__ void prefetch_l2(const void *p, unsigned int bytes)
@@ -1072,14 +1077,13 @@ __device__ __forceinline__ void prefetch_l2(const void *p, unsigned int bytes)
 #endif
 #define CLODE_REPLAY_PF_ROWS 4
 
-// The replay launch has the recording launch's grid (a warp per region), so
-// its blocks must fit on an SM as many at a time as the recording launch's:
-// with a program register cap (CLODE_MAXNREG) the replay takes the same cap;
-// without one, a cap that keeps the observer state in registers.
+// The replay launch has the recording launch's number of blocks, each
+// replay warp taking one or more regions (rec_regions_per_warp, chosen by
+// the host so that the replay's blocks fit on an SM as many at a time as
+// the recording launch's): its own register cap keeps the observer state
+// in registers.
 #ifndef CLODE_REPLAY_MAXNREG
-#if defined(CLODE_MAXNREG)
-#define CLODE_REPLAY_MAXNREG CLODE_MAXNREG
-#elif defined(CLODE_DOUBLE_PRECISION)
+#if defined(CLODE_DOUBLE_PRECISION)
 #define CLODE_REPLAY_MAXNREG 255
 #elif CLODE_PRECISE
 #define CLODE_REPLAY_MAXNREG 216
@@ -1259,12 +1263,10 @@ __device__ __forceinline__ void column_load(const realtype *r, realtype &t, real
 // reads them from global memory, the rows a few steps ahead prefetched
 // into L2.
 template <bool STAGED>
-__device__ __forceinline__ void features_replay(const Args &a)
+__device__ __forceinline__ void replay_region(const Args &a, const unsigned long long warp, Counters &c)
 {
     extern __shared__ __align__(128) unsigned char replay_smem[];
-    Counters c = {0, 0, 0, 0};
     const unsigned int lane = threadIdx.x & 31u;
-    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long R = a.rec_rows;
     const unsigned long long rows = a.rec_used[warp];
     const unsigned int row_bytes = CLODE_REC_FIELDS * 32u * (unsigned int)sizeof(realtype);
@@ -1284,6 +1286,7 @@ __device__ __forceinline__ void features_replay(const Args &a)
         // rows [0, issued) and mask chunks [0, chunks_issued) have been requested
         unsigned long long issued = 0, chunks_issued = 0;
         const unsigned long long chunks = (rows + 15) / 16;
+        __syncwarp();  // (a warp's previous region is done with the stages)
         if (lane == 0 && rows > 0) {
             for (unsigned int k = 0; k < S + 2; ++k)
                 bar_init(s_bars + 8u * k);
@@ -1355,6 +1358,13 @@ __device__ __forceinline__ void features_replay(const Args &a)
             }
             __syncwarp();
         }
+        // every copy of this region has completed: the barriers are released
+        // for the warp's next region
+        __syncwarp();
+        if (lane == 0 && rows > 0) {
+            for (unsigned int k = 0; k < S + 2; ++k)
+                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(s_bars + 8u * k) : "memory");
+        }
     } else {
         // the first rows of the region into L2 (R is a multiple of 16, so every
         // region's masks start on a 16-byte boundary)
@@ -1391,6 +1401,20 @@ __device__ __forceinline__ void features_replay(const Args &a)
             replay_row(L, a, warp, lane, vmask, smask, t, x, dx, aux, c);
         }
     }
+}
+
+// A replay warp takes rec_regions_per_warp consecutive regions in turn, so
+// that a replay block of blockDim.x threads covers the regions of a
+// recording block of rec_regions_per_warp times as many: the replay's
+// registers are not bound by the recording launch's residency.
+template <bool STAGED>
+__device__ __forceinline__ void features_replay(const Args &a)
+{
+    Counters c = {0, 0, 0, 0};
+    const unsigned long long w = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned int k = a.rec_regions_per_warp > 0 ? a.rec_regions_per_warp : 1u;
+    for (unsigned int j = 0; j < k; ++j)
+        replay_region<STAGED>(a, w * k + j, c);
     flush_counters(a, c);
 }
 
@@ -1402,6 +1426,20 @@ extern "C" __global__ void __maxnreg__(CLODE_REPLAY_MAXNREG) clode_features_repl
 extern "C" __global__ void __maxnreg__(CLODE_REPLAY_MAXNREG) clode_features_replay_staged(const Args a)
 {
     features_replay<true>(a);
+}
+
+// Recording and replay in one launch: each warp records its region, then
+// replays it (rows from global memory), so that a warp whose region is done
+// replays it while others still record, and a launch pair has one end
+// instead of two.  The warp's lanes wrote every row, mask, member list entry
+// and finish block it reads: __syncwarp orders those writes before the reads.
+extern "C" __global__ void CLODE_CAP clode_features_record_replay(const Args a)
+{
+    record_body(a);
+    __syncwarp();
+    Counters c = {0, 0, 0, 0};
+    replay_region<false>(a, ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5, c);
+    flush_counters(a, c);
 }
 #endif  // !CLODE_FEATURE_STORE
 #endif  // CLODE_HAVE_OBSERVER

@@ -209,6 +209,7 @@ struct clode_sim {
     cudaKernel_t kp_transient = nullptr, kp_trajectory = nullptr, kp_features = nullptr;
     cudaKernel_t kp_init_rec = nullptr, kp_replay = nullptr;  // replay of the warm-up pass
     cudaKernel_t kp_replay_staged = nullptr;                  // ... through shared-memory stages
+    cudaKernel_t kp_record_replay = nullptr;                  // recording and replay in one launch
     unsigned int fin_words = 0, rec_fields = 0;
     int last_grid = 0, last_block = 0;
     unsigned int obs_words = 0;
@@ -257,8 +258,10 @@ struct clode_sim {
     int replay_stages = 0;      // shared-memory row stages per replay warp (0: rows read from global memory;
                                 // -1: up to 4 that fit)
     double replay_cap_scale = 1.0;  // autotuner trials on a sample: the regions' memory scaled by its fraction
-    bool replay_split = true;   // rows of the observer's event fields, the pass's sums taken while recording
+    bool replay_split = false;  // rows of the observer's event fields, the pass's sums taken while recording
+    bool replay_fused = false;  // recording and replay in one launch per launch pair
     unsigned int last_stages = 0;          // stages the last replayed run used
+    unsigned int last_regions_per_warp = 0;  // regions each replay warp of the last replayed run took
     unsigned int last_rewarm = 0;          // of last_fallback: members whose warm-up was run again
     double last_rows = 0.0;                // rows the last replayed run recorded (all regions, all launches)
     double last_warmup_ms = 0.0;           // the separate warm-up launch of the last integrated features run
@@ -519,7 +522,7 @@ struct clode_sim {
             check_cuda(cudaLibraryGetKernel(&kp_trajectory, lib, "clode_trajectory_persistent"),
                        "kernel clode_trajectory_persistent");
             k_init = kp_init = k_features = kp_features = nullptr;
-            kp_init_rec = kp_replay = kp_replay_staged = nullptr;
+            kp_init_rec = kp_replay = kp_replay_staged = kp_record_replay = nullptr;
             obs_words = 0;
             if (kind == CLODE_SIM_FEATURES) {
                 check_cuda(cudaLibraryGetKernel(&k_init, lib, "clode_init_observer"), "kernel clode_init_observer");
@@ -540,6 +543,8 @@ struct clode_sim {
                                "kernel clode_features_replay");
                     check_cuda(cudaLibraryGetKernel(&kp_replay_staged, lib, "clode_features_replay_staged"),
                                "kernel clode_features_replay_staged");
+                    check_cuda(cudaLibraryGetKernel(&kp_record_replay, lib, "clode_features_record_replay"),
+                               "kernel clode_features_record_replay");
                     check_cuda(cudaLibraryGetGlobal(&gp, &gb, lib, "clode_finish_words"), "finish block size");
                     check_cuda(cudaMemcpy(&fin_words, gp, sizeof fin_words, cudaMemcpyDeviceToHost),
                                "finish block size");
@@ -1131,12 +1136,48 @@ struct clode_sim {
         return 0;
     }
 
+    // The replay launch's shape for a recording launch of `grid` blocks of
+    // `block` threads: the same number of blocks, each of block / k threads
+    // whose warps take k regions in turn, for the smallest k (1, 2, 4) whose
+    // blocks fit on an SM as many at a time as the recording launch's (the
+    // replay's own register cap then never makes its regions wait for a
+    // second wave); and its shared-memory stages at that block size.
+    void replay_shape(unsigned int grid, unsigned int block, unsigned int row_bytes, unsigned int &k,
+                      unsigned int &rblock, unsigned int &stages, size_t &smem)
+    {
+        int sms = 1;
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count");
+        const unsigned long long rec_per_sm = ((unsigned long long)grid + sms - 1) / std::max(sms, 1);
+        k = 1;
+        rblock = block;
+        stages = 0;
+        smem = 0;
+        for (unsigned int kk = 1; kk <= 4; kk *= 2) {
+            if (block % (32u * kk) != 0)
+                break;
+            const unsigned int rb = block / kk;
+            size_t sm = 0;
+            const unsigned int st = replay_stage_count(grid, rb, row_bytes, sm);
+            int per_sm = 0;
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                           &per_sm, (const void *)(st >= 2 ? kp_replay_staged : kp_replay), (int)rb, sm),
+                       "replay occupancy query");
+            k = kk;
+            rblock = rb;
+            stages = st;
+            smem = sm;
+            if ((unsigned long long)per_sm >= rec_per_sm)
+                return;
+        }
+    }
+
     // false (nothing launched) when the memory for the regions is too small
     template <typename R>
     bool replay_run(long long positions)
     {
+        const bool fused = replay_fused && kp_record_replay;
         unsigned int grid = 0, block = 0;
-        persistent_shape(kp_init_rec, positions, grid, block);
+        persistent_shape(fused ? kp_record_replay : kp_init_rec, positions, grid, block);
         const unsigned long long warps = (unsigned long long)grid * block / 32;
         const size_t rs = sizeof(R);
         // bytes per warp-wide row: every field of 32 lanes and the two masks
@@ -1180,7 +1221,9 @@ struct clode_sim {
         fallback_count.reserve(2 * sizeof(unsigned int));
         rec_err.reserve(sizeof(unsigned int));
         size_t stage_smem = 0;
-        const unsigned int stages = replay_stage_count(grid, block, (unsigned int)(rec_fields * 32u * rs), stage_smem);
+        unsigned int stages = 0, per_warp = 1, rblock = block;
+        if (!fused)
+            replay_shape(grid, block, (unsigned int)(rec_fields * 32u * rs), per_warp, rblock, stages, stage_smem);
         // a warp takes no new member once its region is this full: the members
         // it holds then must still fit (2.5 times the average member's steps)
         double spm = replay_steps_per_member;
@@ -1201,6 +1244,7 @@ struct clode_sim {
         a.fallback_count = fallback_count.as<unsigned int>();
         a.rec_stages = stages;
         a.rec_error = rec_err.as<unsigned int>();
+        a.rec_regions_per_warp = per_warp;
         auto set_regions = [&]() {
             a.rec = rec.as<R>();
             a.rec_mask = rec_mask.as<unsigned int>();
@@ -1230,9 +1274,14 @@ struct clode_sim {
         };
         for (;;) {
             check_cuda(cudaEventRecord(rev[0], stream), "event record");
-            launch_args(kp_init_rec, grid, block, a);
-            check_cuda(cudaEventRecord(rev[1], stream), "event record");
-            launch_args(stages >= 2 ? kp_replay_staged : kp_replay, grid, block, a, stage_smem);
+            if (fused) {
+                launch_args(kp_record_replay, grid, block, a);
+                check_cuda(cudaEventRecord(rev[1], stream), "event record");
+            } else {
+                launch_args(kp_init_rec, grid, block, a);
+                check_cuda(cudaEventRecord(rev[1], stream), "event record");
+                launch_args(stages >= 2 ? kp_replay_staged : kp_replay, grid, rblock, a, stage_smem);
+            }
             check_cuda(cudaEventRecord(rev[2], stream), "event record");
             ++chunks;
             check_cuda(cudaMemcpyAsync(&taken, work.p, sizeof taken, cudaMemcpyDeviceToHost, stream),
@@ -1313,6 +1362,7 @@ struct clode_sim {
         last_fallback = nfb + nrw;
         last_rewarm = nrw;
         last_stages = stages;
+        last_regions_per_warp = per_warp;
         if (spm > 0.0)
             replay_steps_per_member = spm;
         return true;
@@ -1733,6 +1783,36 @@ struct clode_sim {
                 best = last_ms;
             else
                 replay = base_replay;
+            // the replay's row layout (a rebuild) and its launch layout
+            if (replay) {
+                const bool base_split = replay_split;
+                replay_split = !base_split;
+                built = false;
+                try {
+                    ensure_built();
+                    run_trial();
+                } catch (...) {
+                    replay_split = base_split;
+                    built = false;
+                    throw;
+                }
+                log_msg(CLODE_LOG_INFO, "autotune: replay_split=%d: %.3f ms", (int)replay_split, last_ms);
+                if (last_ms < best) {
+                    best = last_ms;
+                } else {
+                    replay_split = base_split;
+                    built = false;
+                    ensure_built();
+                }
+                const bool base_fused = replay_fused;
+                replay_fused = !base_fused;
+                run_trial();
+                log_msg(CLODE_LOG_INFO, "autotune: replay_fused=%d: %.3f ms", (int)replay_fused, last_ms);
+                if (last_ms < best)
+                    best = last_ms;
+                else
+                    replay_fused = base_fused;
+            }
         }
         // fused or separate observer initialisation (two-pass observers)
         if (kind == CLODE_SIM_FEATURES && obs_two_pass()) {
@@ -2455,6 +2535,8 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 sim->replay_split = value != 0.0;
                 sim->built = false;
             }
+        } else if (k == "replay_fused") {
+            sim->replay_fused = value != 0.0;
         } else if (k == "replay_stages") {
             if (value < -1.0 || value > 16.0)
                 fail(CLODE_ERR_INVALID_ARGUMENT, "replay_stages must be -1 (automatic) or 0 .. 16");
@@ -2496,7 +2578,9 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "replay_mb") *value = sim->replay_mb;
         else if (k == "replay_stages") *value = sim->replay_stages;
         else if (k == "replay_split") *value = sim->replay_split;
+        else if (k == "replay_fused") *value = sim->replay_fused;
         else if (k == "replay_stages_used") *value = sim->last_stages;
+        else if (k == "replay_regions_per_warp") *value = sim->last_regions_per_warp;
         else if (k == "replay_rewarm") *value = sim->last_rewarm;
         else if (k == "replay_rows") *value = sim->last_rows;
         else if (k == "replay_row_bytes")  // one warp-wide row: every stored field of 32 lanes and the two masks

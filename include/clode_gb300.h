@@ -308,6 +308,14 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * pass in device memory and the feature pass replays them into the observer
  * instead of integrating the trajectory again; results are identical;
  * setting it to 0 frees the device memory of the stored steps),
+ * "replay_split" (0, the default: a stored row holds t, x, dx and aux and the
+ * replay runs the observer's whole feature-pass update; 1: a row holds only
+ * the fields the observer's warm-up-dependent logic reads, and the recording
+ * launch takes the rest of the pass (extent, means, step statistics) and
+ * leaves it in the member's finish block; not with "precise"; results are
+ * identical; a rebuild), "replay_fused" (0, the default; 1: each warp
+ * records its region and replays it in one launch per launch pair; results
+ * are identical),
  * "replay_stages" (0, the default: the replay reads each stored row from
  * global memory; 2 .. 16: it copies rows that many ahead into shared memory
  * with bulk copies, one per row, completing on mbarriers; -1: up to 4 that
@@ -323,7 +331,9 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * "replay_fallback" (members given to the plain passes), "replay_rewarm" (of
  * those, members whose warm-up a full region cut short), "replay_rows" (rows
  * recorded), "replay_row_bytes" (bytes of one warp-wide row of the built
- * program), "replay_stages_used", "warmup_ms" (the separate warm-up launch
+ * program), "replay_stages_used", "replay_regions_per_warp" (regions each
+ * replay warp took: more than one when the replay's blocks fit on an SM
+ * fewer at a time than the recording launch's), "warmup_ms" (the separate warm-up launch
  * of the last integrated features run),
  * "replay_record_ms", "replay_replay_ms", "replay_fallback_ms" (device time
  * of each launch kind).

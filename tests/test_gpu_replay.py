@@ -11,6 +11,9 @@ cases that exercise each path of the replay:
 * steppers fixed and adaptive, FP32 and FP64, per-member time spans;
 * the replay's rows straight from global memory (the default) and through
   shared-memory stages (``replay_stages`` 2 and 8: TMA bulk copies);
+* whole rows (``replay_split`` 0) and replay warps that take several regions
+  (more recording blocks per SM than the replay's registers allow);
+* recording and replay in one launch per launch pair (``replay_fused``);
 * record regions far too small for the ensemble (``replay_mb``): many
   recording launches, members still running when their region fills (the
   plain warm-up and feature passes run them again);
@@ -94,6 +97,15 @@ def test_replay_equals_integrated_feature_pass(observer, stepper, single):
     assert on.get_stats()["rhs_evals"] < 0.75 * off.get_stats()["rhs_evals"]
 
 
+@pytest.mark.parametrize("split", [1, 0])
+def test_recording_and_replay_in_one_launch(split):
+    x0, pars, ts = _lorenz(20000, seed=13)
+    on = _sim("nhood2", "dopri5", True, 1, {"replay_fused": 1, "replay_split": split, "replay_mb": 200})
+    off = _sim("nhood2", "dopri5", True, 0)
+    _equal(_run(on, x0, pars, ts), _run(off, x0, pars, ts))
+    assert on.get_option("replay_chunks") >= 1
+
+
 @pytest.mark.parametrize("stages", [0, 2, 8])
 def test_rows_from_global_memory_or_stages(stages):
     x0, pars, ts = _lorenz(3000, seed=11)
@@ -101,6 +113,18 @@ def test_rows_from_global_memory_or_stages(stages):
     off = _sim("nhood2", "dopri5", True, 0)
     _equal(_run(on, x0, pars, ts), _run(off, x0, pars, ts))
     assert on.get_option("replay_stages_used") == stages
+
+
+def test_replay_warps_take_several_regions():
+    # 8 recording blocks of 128 threads per SM: the replay (its own register
+    # cap) fits fewer, so each replay warp takes two or more regions; whole
+    # rows (replay_split 0) with the replay running the whole update
+    x0, pars, ts = _lorenz(160000, seed=12)
+    ts[:, 1] = np.minimum(ts[:, 1], 8.0)
+    on = _sim("nhood2", "dopri5", True, 1, {"blocks_per_sm": 8, "replay_split": 0})
+    off = _sim("nhood2", "dopri5", True, 0)
+    _equal(_run(on, x0, pars, ts), _run(off, x0, pars, ts))
+    assert on.get_option("replay_regions_per_warp") >= 2
 
 
 def test_small_regions_many_launches_and_overflow():
