@@ -293,11 +293,12 @@ def bench_trajectory(args, tuned_options: dict) -> dict:
     n = pars.shape[0]
     sim.set_problem_data(np.zeros(n), pars.flatten(order="F"))
     sim.set_tspan([0.0, steps * 1e-3])
-    times = []
+    times, draws = [], []
     for rep in range(3):
         sim.seed_rng(args.seed + rep)
         sim.trajectory()
         times.append(sim.last_kernel_ms())
+        draws.append(sim.get_option("predraw_ms"))
     rows = int(np.asarray(sim.get_n_stored()).max()) + 1
     ms = float(min(times))
     written = rows * n * 3 * 4
@@ -314,6 +315,7 @@ def bench_trajectory(args, tuned_options: dict) -> dict:
             "workload": f"OU trajectories, 65536 members (256 parameter points x 256 realisations), seuler "
                         f"dt 1e-3 over [0, {steps * 1e-3:g}], (t, x, dx) stored every 10 steps, FP32",
             "members": n, "steps_per_member": steps, "rows": rows, "ms": ms, "ms_all": times,
+            "predrawn": bool(sim.get_option("predrawn")), "predraw_ms": draws[int(np.argmin(times))],
             "member_steps_per_s": n * steps / (ms / 1e3),
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
                          "traffic": None, "algorithmic_bytes": written,
@@ -441,10 +443,10 @@ def bench_configs(args, tuned_options: dict) -> dict:
         sim.set_option(k, v)
     sim.set_solver_params(W.SolverParams(dt=1e-3, dtmax=1.0, abstol=1e-9, reltol=1e-6, max_steps=1000000))
     # this map's own tuning (a cheap right-hand side: whether replaying the
-    # stored steps pays is the autotuner's call), on a strided sample
+    # stored steps pays is the autotuner's call), on the whole map
     sim.set_problem_data(x0.flatten(order="F"), pars.flatten(order="F"))
     sim.set_tspan([0.0, 500.0])
-    tuned_lorenz = sim.autotune(131072)
+    tuned_lorenz = sim.autotune(0)
     times = []
     for _ in range(3):
         sim.set_problem_data(x0.flatten(order="F"), pars.flatten(order="F"))  # same size: dt continues
@@ -504,13 +506,26 @@ def bench_feature_store(args, tuned_options: dict) -> dict:
         ms = plain.last_kernel_ms()
         traj.trajectory()
         t_sep.append(ms + traj.last_kernel_ms())
-    same = bool(np.array_equal(store.get_n_stored(), traj.get_n_stored()))
+    same_fast = bool(np.array_equal(store.get_n_stored(), traj.get_n_stored()))
+    # identity of the stored rows, in the exact build (with fmad the compiler
+    # may contract multiply-adds differently in the two kernels, so the fast
+    # build's step sequences may part by a rounding)
+    exact = {"fmad": 0, "prec_div": 1, "ftz": 0}
+    store_x = setup(W.FeatureSimulatorBase(pi, "dopri5", "nhood2", op, True, W.OpenCLResource(), ""))
+    traj_x = setup(W.TrajectorySimulatorBase(pi, "dopri5", True, W.OpenCLResource(), ""), traj=True)
+    for sim in (store_x, traj_x):
+        for k, v in exact.items():
+            sim.set_option(k, v)
+    store_x.features_store(True, event_rows=16)
+    traj_x.trajectory()
+    same = bool(np.array_equal(store_x.get_n_stored(), traj_x.get_n_stored())
+                and np.array_equal(np.asarray(store_x.get_x()), np.asarray(traj_x.get_x())))
     return {"workload": f"lactotroph nhood2, {grid}x{grid} (gcal, gbk) grid, tspan [0, 3000] ms, DP45 rtol 1e-6 "
                         "FP32, a row every 50 steps, 16 event states per member",
             "members": grid * grid, "rows_max": int(store.get_n_stored().max()) + 1,
             "events_max": int(store.get_n_events().max()),
             "one_pass_ms": min(t_store), "two_runs_ms": min(t_sep), "speedup": min(t_sep) / min(t_store),
-            "rows_identical_to_trajectory_run": same}
+            "rows_identical_to_trajectory_run": same, "rows_identical_fast_build": same_fast}
 
 
 def bench_reference_arm(args):
@@ -576,8 +591,9 @@ def main():
     ap.add_argument("--replay-stages", type=int, default=None,
                     help="shared-memory row stages of the replay (-1 automatic, the engine default; 0: rows read "
                          "from global memory)")
-    ap.add_argument("--autotune", type=int, default=1048576,
-                    help="autotune on a strided sample of this many members first (0: off)")
+    ap.add_argument("--autotune", type=int, default=4194304,
+                    help="autotune on a strided sample of this many members first (0: off; the default, the "
+                         "whole 2048 x 2048 map: a smaller sample mispredicts the map by a few percent)")
     ap.add_argument("--surrogate-grid", type=int, default=4096)
     ap.add_argument("--surrogate-steps", type=int, default=3000)
     ap.add_argument("--surrogate-batch", type=int, default=4096)

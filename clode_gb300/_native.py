@@ -134,6 +134,8 @@ SIGNATURES = {
     "clode_sim_get_option": (C.c_int, [_P, C.c_char_p, C.POINTER(C.c_double)]),
     "clode_sim_kernel_info": (C.c_int, [_P, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "clode_launch_count": (C.c_ulonglong, []),
+    "clode_rng_jump": (C.c_int, [C.c_ulonglong, C.c_ulonglong, C.c_ulonglong, C.POINTER(C.c_ulonglong),
+                                 C.POINTER(C.c_ulonglong)]),
     "clode_sim_features_noalloc": (C.c_int, [_P, C.c_longlong, _P, _P, _P, C.POINTER(C.c_ulonglong), _P, _P, _P,
                                              _P, C.POINTER(C.c_int), _P]),
     "clode_sim_autotune": (C.c_int, [_P, C.c_longlong, C.POINTER(C.c_double)]),

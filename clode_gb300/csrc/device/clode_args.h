@@ -130,6 +130,16 @@ struct ArgsT {
     // regions each replay warp takes in turn (the replay's blocks are the
     // recording launch's, with this many times fewer threads)
     unsigned int rec_regions_per_warp;
+    // pre-drawn normal deviates (stochastic stepper): member i's k-th deviate
+    // is noise[i * noise_stride + k]; null: the kernels draw them.  Filled by
+    // the draw launch from noise_count[i] (the deviates member i's run takes,
+    // from the count launch), the generator's jump matrices noise_mats and
+    // noise_block candidates per lane and round.
+    R *noise;
+    unsigned long long noise_stride;
+    unsigned int *noise_count;
+    const unsigned long long *noise_mats;
+    unsigned int noise_block;
     SolverParamsT<R> sp;
     ObserverParamsT<R> op;
 };

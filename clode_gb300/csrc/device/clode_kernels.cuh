@@ -91,9 +91,10 @@ __device__ __forceinline__ void member_load(Member &m, const Args &a, int i, Cou
     m.r.have_spare = false;
     m.r.spare = ZERO;
     m.sqdt = sqrt(m.dt);
+    m.noise = a.noise ? a.noise + (unsigned long long)i * a.noise_stride : nullptr;
 #pragma unroll
     for (int j = 0; j < N_WIENER; ++j)
-        m.w[j] = rng_normal(m.r) / m.sqdt;
+        m.w[j] = draw_normal(m) / m.sqdt;
 #endif
     getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
     c.rhs += 1;
@@ -109,8 +110,10 @@ __device__ __forceinline__ void member_store(const Member &m, const Args &a, int
     for (int j = 0; j < N_VAR; ++j)
         a.xf[j * n + i] = m.x[j];
 #if CLODE_STOCHASTIC
-    a.rng[i] = m.r.s0;
-    a.rng[n + i] = m.r.s1;
+    if (!a.noise) {  // with pre-drawn deviates the draw launch stored the final RNG words
+        a.rng[i] = m.r.s0;
+        a.rng[n + i] = m.r.s1;
+    }
 #endif
     a.dt[i] = m.dt;
     a.tf[i] = m.t;
@@ -419,6 +422,136 @@ extern "C" __global__ void CLODE_CAP clode_trajectory_persistent(const Args a)
     }
     flush_counters(a, c);
 }
+
+#if CLODE_STOCHASTIC
+// ------------------------------------------------- pre-drawn deviates --
+// A stochastic trajectory run draws its members' normal deviates in two
+// launches before it integrates: the count launch replays each member's
+// step loop on time alone (run_trajectory's conditions: t <= t1, max_steps,
+// max_store) to find how many deviates the member takes (one per noise
+// variable at the start and per step); the draw launch then produces each
+// member's deviates in order, with CLODE_NOISE_LANES lanes per member.  The
+// member's stream is cut into blocks of noise_block candidates of the polar
+// method (two uniforms each); lane l starts at block l (the stream jumped
+// ahead by l blocks, a GF(2) matrix of the generator, noise_mats[l - 1]) and
+// after each round jumps L blocks on (noise_mats[L - 1]).  A round takes
+// two passes over the lane's block: the first counts its accepted
+// candidates, a scan over the member's lanes gives each lane the index of
+// its first pair, the second writes the pairs the member takes.  The
+// deviates and the final RNG words (the stream after the candidate of the
+// last pair taken; an unused second deviate of that pair is the reference's
+// cache, dropped at the end of a launch) are those of drawing in the
+// integration loop.  Rejected candidates cost nothing beyond their own
+// draws, and four lanes per member run where one did.
+#define CLODE_NOISE_LANES 4
+
+extern "C" __global__ void clode_noise_count(const Args a)
+{
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (unsigned long long)a.nPts)
+        return;
+    Member m;
+    m.t = member_t0(a, (int)i);
+    m.tlo = ZERO;
+    const realtype dt = a.dt[i], t1 = member_t1(a, (int)i);
+    unsigned int step = 0, to_store = a.sp.nout;
+    unsigned long long row = 0;
+    while (t_le(m, t1) && step < a.sp.max_steps && row < (unsigned long long)a.sp.max_store) {
+        ++step;
+        advance_time(m.t, m.tlo, dt);
+        if (--to_store == 0) {
+            to_store = a.sp.nout;
+            ++row;
+        }
+    }
+    a.noise_count[i] = (step + 1u) * (unsigned int)N_WIENER;
+}
+
+// the stream state (s0, s1) times a jump matrix (128 columns of two words)
+__device__ __forceinline__ void jump_apply(const unsigned long long (*m)[2], unsigned long long &s0,
+                                           unsigned long long &s1)
+{
+    unsigned long long r0 = 0ull, r1 = 0ull;
+#pragma unroll 16
+    for (int c = 0; c < 64; ++c) {
+        const unsigned long long k = 0ull - ((s0 >> c) & 1ull);
+        r0 ^= m[c][0] & k;
+        r1 ^= m[c][1] & k;
+    }
+#pragma unroll 16
+    for (int c = 0; c < 64; ++c) {
+        const unsigned long long k = 0ull - ((s1 >> c) & 1ull);
+        r0 ^= m[64 + c][0] & k;
+        r1 ^= m[64 + c][1] & k;
+    }
+    s0 = r0;
+    s1 = r1;
+}
+
+extern "C" __global__ void clode_noise_draw(const Args a)
+{
+    constexpr unsigned int L = CLODE_NOISE_LANES;
+    __shared__ unsigned long long mats[L][128][2];
+    for (unsigned int k = threadIdx.x; k < L * 256u; k += blockDim.x)
+        (&mats[0][0][0])[k] = a.noise_mats[k];
+    __syncthreads();
+    const unsigned long long n = (unsigned long long)a.nPts;
+    const unsigned long long i = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) / L;
+    const unsigned int l = threadIdx.x % L;  // blockDim.x is a multiple of 32: a member's lanes share a warp
+    const bool live = i < n;
+    const unsigned int P = live ? (a.noise_count[i] + 1u) / 2u : 0u;  // pairs the member takes
+    Rng r;
+    r.s0 = live ? a.rng[i] : 0ull;
+    r.s1 = live ? a.rng[n + i] : 0ull;
+    if (l > 0 && P > 0)
+        jump_apply(mats[l - 1], r.s0, r.s1);
+    realtype *out = live ? a.noise + i * a.noise_stride : nullptr;
+    const unsigned int C = a.noise_block;
+    unsigned int done = 0;  // pairs the member's lanes have produced (the same in its lanes)
+    while (__any_sync(0xffffffffu, done < P)) {
+        const bool need = done < P;
+        unsigned int cnt = 0;
+        if (need) {
+            Rng q = r;
+            for (unsigned int c = 0; c < C; ++c) {
+                realtype u, v;
+                if (polar_candidate(q, u, v) < ONE)
+                    ++cnt;
+            }
+        }
+        unsigned int incl = cnt;
+#pragma unroll
+        for (unsigned int off = 1; off < L; off <<= 1) {
+            const unsigned int t = __shfl_up_sync(0xffffffffu, incl, off, L);
+            if (l >= off)
+                incl += t;
+        }
+        const unsigned int total = __shfl_sync(0xffffffffu, incl, L - 1, L);
+        unsigned int p = done + incl - cnt;  // this lane's first pair
+        if (need && p < P) {
+            Rng q = r;
+            for (unsigned int c = 0; c < C && p < P; ++c) {
+                realtype u, v;
+                const realtype s = polar_candidate(q, u, v);
+                if (s < ONE) {
+                    realtype y1, y2;
+                    polar_pair(u, v, s, y1, y2);
+                    out[2ull * p] = y1;  // the buffer holds 2P deviates per member
+                    out[2ull * p + 1] = y2;
+                    if (p == P - 1) {
+                        a.rng[i] = q.s0;
+                        a.rng[n + i] = q.s1;
+                    }
+                    ++p;
+                }
+            }
+        }
+        done += total;
+        if (need)
+            jump_apply(mats[L - 1], r.s0, r.s1);
+    }
+}
+#endif  // CLODE_STOCHASTIC
 
 #if CLODE_HAVE_OBSERVER
 // --------------------------------------------------- parked observer state --

@@ -43,6 +43,23 @@ __device__ __forceinline__ realtype rng_uniform(Rng &r)
     return mul_rn((realtype)rng_next(r), RCONST(5.421010862427522e-20));
 }
 
+// one candidate of the polar method: (u, v) from two uniforms, and s =
+// u^2 + v^2; the candidate is accepted when s < 1
+__device__ __forceinline__ realtype polar_candidate(Rng &r, realtype &u, realtype &v)
+{
+    u = add_rn(mul_rn(RCONST(2.0), rng_uniform(r)), -ONE);
+    v = add_rn(mul_rn(RCONST(2.0), rng_uniform(r)), -ONE);
+    return add_rn(mul_rn(u, u), mul_rn(v, v));
+}
+
+// the two deviates of an accepted candidate, in the order they are used
+__device__ __forceinline__ void polar_pair(realtype u, realtype v, realtype s, realtype &y1, realtype &y2)
+{
+    const realtype m = sqrt((-RCONST(2.0) * log(s)) / s);
+    y1 = u * m;
+    y2 = v * m;
+}
+
 __device__ __forceinline__ realtype rng_normal(Rng &r)
 {
     if (r.have_spare) {
@@ -51,14 +68,12 @@ __device__ __forceinline__ realtype rng_normal(Rng &r)
     }
     realtype u, v, s;
     do {
-        u = add_rn(mul_rn(RCONST(2.0), rng_uniform(r)), -ONE);
-        v = add_rn(mul_rn(RCONST(2.0), rng_uniform(r)), -ONE);
-        s = add_rn(mul_rn(u, u), mul_rn(v, v));
+        s = polar_candidate(r, u, v);
     } while (s >= ONE);
-    realtype m = sqrt((-RCONST(2.0) * log(s)) / s);
-    r.spare = v * m;
+    realtype y1;
+    polar_pair(u, v, s, y1, r.spare);
     r.have_spare = true;
-    return u * m;
+    return y1;
 }
 
 }  // namespace clode

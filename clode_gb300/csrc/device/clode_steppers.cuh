@@ -87,8 +87,20 @@ struct Member {
     Rng r;
 #if CLODE_STOCHASTIC
     realtype sqdt;  // sqrt(dt), fixed for the whole launch: the stochastic stepper never changes dt
+    const realtype *noise;  // this member's pre-drawn deviates, next first (null: drawn here)
 #endif
 };
+
+#if CLODE_STOCHASTIC
+// the member's next normal deviate: pre-drawn by the draw launch, or drawn
+// from its stream here (the same sequence either way)
+__device__ __forceinline__ realtype draw_normal(Member &m)
+{
+    if (m.noise)
+        return *m.noise++;
+    return rng_normal(m.r);
+}
+#endif
 
 // per-thread work counters, summed into ArgsT::stats at the end of a member
 struct Counters {
@@ -211,7 +223,7 @@ __device__ __forceinline__ int step_member(Member &m, const SolverParams &sp, co
 #if CLODE_STOCHASTIC
 #pragma unroll
     for (int j = 0; j < N_WIENER; ++j)
-        m.w[j] = rng_normal(m.r) / m.sqdt;  // randn / sqrt(dt), fixed_explicit_step.clh:29-33
+        m.w[j] = draw_normal(m) / m.sqdt;  // randn / sqrt(dt), fixed_explicit_step.clh:29-33
 #endif
     getRHS(m.t, m.x, m.p, m.dx, m.aux, m.w);
     c.steps++;

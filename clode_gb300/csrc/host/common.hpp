@@ -74,7 +74,7 @@ struct NoallocFeaturesLaunch {
     int n_par;             // parameter columns the kernel reads from pars
     int device;
     int block;
-    unsigned char args[512];  // ArgsT<float> or ArgsT<double>
+    unsigned char args[768];  // ArgsT<float> or ArgsT<double>
 };
 }  // namespace clode
 

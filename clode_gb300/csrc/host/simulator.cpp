@@ -6,6 +6,7 @@
 // RNG seeding, dt persistence for adaptive continuation, lazy observer
 // initialisation and the x0/tspan shifts for continuation runs.
 #include "common.hpp"
+#include "rng_jump.hpp"
 #include "../device/clode_args.h"
 
 #include <algorithm>
@@ -197,6 +198,9 @@ struct clode_sim {
     // rows used per region, finish blocks, fallback list and its length
     DevBuf rec, rec_mask, rec_member, rec_used, fin, fallback, fallback_count;
     DevBuf rec_err;  // set by the replay when a shared-memory stage was not filled in time
+    // pre-drawn deviates of stochastic trajectory runs: the deviates, each
+    // member's count, the generator's jump matrices
+    DevBuf noise, noise_count, noise_mats;
 
     // program
     bool built = false;
@@ -210,6 +214,7 @@ struct clode_sim {
     cudaKernel_t kp_init_rec = nullptr, kp_replay = nullptr;  // replay of the warm-up pass
     cudaKernel_t kp_replay_staged = nullptr;                  // ... through shared-memory stages
     cudaKernel_t kp_record_replay = nullptr;                  // recording and replay in one launch
+    cudaKernel_t k_noise_count = nullptr, k_noise_draw = nullptr;  // pre-drawn deviates (stochastic stepper)
     unsigned int fin_words = 0, rec_fields = 0;
     int last_grid = 0, last_block = 0;
     unsigned int obs_words = 0;
@@ -260,6 +265,12 @@ struct clode_sim {
     double replay_cap_scale = 1.0;  // autotuner trials on a sample: the regions' memory scaled by its fraction
     bool replay_split = false;  // rows of the observer's event fields, the pass's sums taken while recording
     bool replay_fused = false;  // recording and replay in one launch per launch pair
+    bool predraw = false;       // stochastic trajectories: deviates drawn by their own launches first
+    bool noise_on = false;      // make_args: the launch reads the pre-drawn deviates
+    bool last_predrawn = false;
+    double last_draw_ms = 0.0;  // the count and draw launches of the last pre-drawn run
+    unsigned long long noise_stride = 0;
+    unsigned int mats_block = 0;  // candidates per lane and round the jump matrices in noise_mats are for
     unsigned int last_stages = 0;          // stages the last replayed run used
     unsigned int last_regions_per_warp = 0;  // regions each replay warp of the last replayed run took
     unsigned int last_rewarm = 0;          // of last_fallback: members whose warm-up was run again
@@ -306,7 +317,8 @@ struct clode_sim {
         return {&x0,  &pars,   &xf,    &rng,    &dt,   &tf,    &tspan_dev, &odata, &F,
                 &t,   &x,      &dx,    &aux,    &nstored, &status, &stats, &stage, &work,
                 &ev_t, &ev_x, &ev_dx, &ev_aux, &nevents, &order, &order_scratch, &work_counts, &order_work,
-                &rec, &rec_mask, &rec_member, &rec_used, &fin, &fallback, &fallback_count, &rec_err};
+                &rec, &rec_mask, &rec_member, &rec_used, &fin, &fallback, &fallback_count, &rec_err,
+                &noise, &noise_count, &noise_mats};
     }
 
     size_t real_size() const { return single ? sizeof(float) : sizeof(double); }
@@ -523,6 +535,11 @@ struct clode_sim {
                        "kernel clode_trajectory_persistent");
             k_init = kp_init = k_features = kp_features = nullptr;
             kp_init_rec = kp_replay = kp_replay_staged = kp_record_replay = nullptr;
+            k_noise_count = k_noise_draw = nullptr;
+            if (stepper == "seuler") {
+                check_cuda(cudaLibraryGetKernel(&k_noise_count, lib, "clode_noise_count"), "kernel clode_noise_count");
+                check_cuda(cudaLibraryGetKernel(&k_noise_draw, lib, "clode_noise_draw"), "kernel clode_noise_draw");
+            }
             obs_words = 0;
             if (kind == CLODE_SIM_FEATURES) {
                 check_cuda(cudaLibraryGetKernel(&k_init, lib, "clode_init_observer"), "kernel clode_init_observer");
@@ -777,6 +794,10 @@ struct clode_sim {
         a.stats = collect_stats ? stats.as<unsigned long long>() : nullptr;
         a.work_next = work.as<unsigned int>();
         a.time_budget_ns = (unsigned long long)(time_budget_ms * 1e6);
+        if (noise_on) {
+            a.noise = noise.as<R>();
+            a.noise_stride = noise_stride;
+        }
         a.sp.dt = (R)sp.dt;
         a.sp.dtmax = (R)sp.dtmax;
         a.sp.abstol = (R)sp.abstol;
@@ -1520,6 +1541,73 @@ struct clode_sim {
         ev_rows = rows;
     }
 
+    // The deviates of a stochastic trajectory run, drawn before it (the
+    // count and draw launches of clode_kernels.cuh); false (nothing drawn)
+    // when their buffer would take more than half the free device memory,
+    // and the trajectory launch draws them itself.
+    template <typename R>
+    bool predraw_run()
+    {
+        noise_count.reserve((size_t)nPts * sizeof(unsigned int));
+        for (cudaEvent_t &e : rev)
+            if (!e)
+                check_cuda(cudaEventCreate(&e), "cudaEventCreate");
+        ArgsT<R> a = make_args<R>();
+        a.noise_count = noise_count.as<unsigned int>();
+        check_cuda(cudaEventRecord(rev[0], stream), "event record");
+        launch_args(k_noise_count, (unsigned int)((nPts + 255) / 256), 256, a);
+        std::vector<unsigned int> counts((size_t)nPts);
+        check_cuda(cudaMemcpyAsync(counts.data(), noise_count.p, counts.size() * sizeof(unsigned int),
+                                   cudaMemcpyDeviceToHost, stream),
+                   "deviate counts read");
+        check_cuda(cudaStreamSynchronize(stream), "deviate counts");
+        unsigned long long most = 0;
+        for (unsigned int c : counts)
+            most = std::max<unsigned long long>(most, c);
+        const unsigned long long pairs = (most + 1) / 2;
+        if (pairs == 0)
+            return false;
+        const unsigned long long stride = (2 * pairs + 3) & ~3ull;
+        const double bytes = (double)nPts * (double)stride * (double)sizeof(R);
+        size_t fr = 0, tot = 0;
+        check_cuda(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+        if (bytes > 0.5 * ((double)fr + (double)noise.bytes)) {
+            log_msg(CLODE_LOG_INFO, "pre-drawn deviates: %.1f GB exceed half the free device memory; drawing "
+                                    "them in the trajectory launch", bytes / 1e9);
+            noise.release();
+            return false;
+        }
+        noise.reserve((size_t)bytes);
+        // candidates per lane and round: about 16 rounds for the member that
+        // takes the most (4 lanes, 0.785 of the candidates accepted), 32 to 512
+        unsigned int block = (unsigned int)std::min<unsigned long long>(
+            512, std::max<unsigned long long>(32, (unsigned long long)((double)pairs / (4 * 0.785 * 16)) + 1));
+        block = (block + 31) / 32 * 32;
+        if (block != mats_block) {
+            // lane l starts l blocks (2 draws a candidate) into the stream; a round moves 4 blocks on
+            std::vector<uint64_t> m(4 * 256);
+            for (int l = 1; l <= 4; ++l) {
+                const Gf2Mat j = gf2_jump(2ull * block * (unsigned long long)l);
+                memcpy(&m[(size_t)(l - 1) * 256], j.col, sizeof j.col);
+            }
+            noise_mats.reserve(m.size() * sizeof(uint64_t));
+            check_cuda(cudaMemcpyAsync(noise_mats.p, m.data(), m.size() * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                       stream),
+                       "jump matrices upload");
+            check_cuda(cudaStreamSynchronize(stream), "jump matrices upload");
+            mats_block = block;
+        }
+        a.noise = noise.as<R>();
+        a.noise_stride = stride;
+        a.noise_mats = noise_mats.as<unsigned long long>();
+        a.noise_block = block;
+        check_cuda(cudaEventRecord(rev[1], stream), "event record");
+        launch_args(k_noise_draw, (unsigned int)((nPts * 4 + 127) / 128), 128, a);
+        check_cuda(cudaEventRecord(rev[2], stream), "event record");
+        noise_stride = stride;
+        return true;
+    }
+
     void trajectory()
     {
         require_problem();
@@ -1529,9 +1617,26 @@ struct clode_sim {
         ensure_stream();
         resize_trajectory();
         begin_run();
-        launch(k_trajectory, kp_trajectory, 0);
+        last_predrawn = false;
+        if (predraw && k_noise_draw && nWiener > 0 && time_budget_ms <= 0.0 && nPts > 0)
+            last_predrawn = single ? predraw_run<float>() : predraw_run<double>();
+        noise_on = last_predrawn;
+        try {
+            launch(k_trajectory, kp_trajectory, 0);
+        } catch (...) {
+            noise_on = false;
+            throw;
+        }
+        noise_on = false;
         end_run("trajectory");
-        log_msg(CLODE_LOG_DEBUG, "run trajectory");
+        last_draw_ms = 0.0;
+        if (last_predrawn) {
+            float c = 0.0f, d = 0.0f;
+            check_cuda(cudaEventElapsedTime(&c, rev[0], rev[1]), "event timing");
+            check_cuda(cudaEventElapsedTime(&d, rev[1], rev[2]), "event timing");
+            last_draw_ms = (double)c + (double)d;
+        }
+        log_msg(CLODE_LOG_DEBUG, "run trajectory%s", last_predrawn ? " (pre-drawn deviates)" : "");
     }
 
     // Chains: a sequence of runs enqueued back to back on the stream with one
@@ -2254,6 +2359,18 @@ int clode_sim_get_observer_params(clode_sim *sim, clode_observer_params *op)
     });
 }
 int clode_sim_seed_rng(clode_sim *sim, int use_seed, int seed) { SIM_GUARD(sim->seed_rng(use_seed != 0, seed)); }
+
+int clode_rng_jump(unsigned long long s0, unsigned long long s1, unsigned long long steps, unsigned long long *out_s0,
+                   unsigned long long *out_s1)
+{
+    if (!out_s0 || !out_s1)
+        return set_error(CLODE_ERR_INVALID_ARGUMENT, "clode_rng_jump: null output");
+    uint64_t a = s0, b = s1;
+    gf2_apply(gf2_jump(steps), a, b);
+    *out_s0 = a;
+    *out_s1 = b;
+    return CLODE_OK;
+}
 int clode_sim_transient(clode_sim *sim) { SIM_GUARD(sim->transient()); }
 int clode_sim_initialize_observer(clode_sim *sim) { SIM_GUARD(sim->initialize_observer()); }
 int clode_sim_features(clode_sim *sim, int reinitialize) { SIM_GUARD(sim->features(reinitialize)); }
@@ -2535,6 +2652,12 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 sim->replay_split = value != 0.0;
                 sim->built = false;
             }
+        } else if (k == "predraw") {
+            sim->predraw = value != 0.0;
+            if (!sim->predraw) {
+                sim->noise.release();
+                sim->noise_count.release();
+            }
         } else if (k == "replay_fused") {
             sim->replay_fused = value != 0.0;
         } else if (k == "replay_stages") {
@@ -2579,6 +2702,9 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "replay_stages") *value = sim->replay_stages;
         else if (k == "replay_split") *value = sim->replay_split;
         else if (k == "replay_fused") *value = sim->replay_fused;
+        else if (k == "predraw") *value = sim->predraw;
+        else if (k == "predrawn") *value = sim->last_predrawn;
+        else if (k == "predraw_ms") *value = sim->last_draw_ms;
         else if (k == "replay_stages_used") *value = sim->last_stages;
         else if (k == "replay_regions_per_warp") *value = sim->last_regions_per_warp;
         else if (k == "replay_rewarm") *value = sim->last_rewarm;

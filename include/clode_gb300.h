@@ -316,6 +316,11 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * identical; a rebuild), "replay_fused" (0, the default; 1: each warp
  * records its region and replays it in one launch per launch pair; results
  * are identical),
+ * "predraw" (0/1, default 0; 1: a stochastic trajectory run draws its
+ * members' normal deviates in launches of their own before it integrates,
+ * four lanes per member, and the trajectory launch reads them; results, RNG
+ * words included, are identical; read-only "predrawn": whether the last run
+ * did, "predraw_ms": its count and draw launches),
  * "replay_stages" (0, the default: the replay reads each stored row from
  * global memory; 2 .. 16: it copies rows that many ahead into shared memory
  * with bulk copies, one per row, completing on mbarriers; -1: up to 4 that
@@ -361,6 +366,12 @@ int clode_sim_autotune(clode_sim *sim, long long sample, double *best_ms);
 /* Number of kernel launches this library has issued since it was loaded
  * (ensemble kernels and the conversion/seeding kernels alike). */
 unsigned long long clode_launch_count(void);
+/* The per-member random stream's state (s0, s1) advanced by `steps` draws
+ * with the generator's jump matrix (the stream of clode/cpp/clODE_random.cl:
+ * 28-44 is linear over GF(2)); the matrices the pre-drawn deviates of a
+ * stochastic trajectory run use.  No device work; no reference counterpart. */
+int clode_rng_jump(unsigned long long s0, unsigned long long s1, unsigned long long steps,
+                   unsigned long long *out_s0, unsigned long long *out_s1);
 /* features() for callers that cannot allocate device memory.  No counterpart
  * in the reference.  Some callers may not call cudaMalloc once they are
  * running: services whose device memory is partitioned once at start-up,
