@@ -50,12 +50,18 @@ FLOPS_PER_STEP_OBS = 5 * N_VAR + 3 * N_AUX + 6  # nhood2 per-step extrema and me
 # by members; the traffic is per-member state, so it grows in proportion
 DRAM_BYTES_PER_MEMBER = (36643072 + 39959552 + 216447488 + 303181824) / 262144
 # DRAM bytes (read + write) per recorded step of the recording and of the
-# replay launches of a replayed map: ncu dram__bytes_{read,write}.sum of all
-# six launches of each kind (three maps of two launch pairs) of the default
-# build on the 512 x 512 case, divided by the three maps' steps (3 x
-# 1,463,676,130); the traffic is the stored rows, so it grows with the steps
-REC_DRAM_BYTES_PER_STEP = (10699342336 + 110497920768) / (3 * 1463676130)
-REPLAY_DRAM_BYTES_PER_STEP = (113871344384 + 1407749888) / (3 * 1463676130)
+# replay launches of a replayed map, by row layout (replay_split 0: whole
+# rows of 1288 bytes per warp; 1: the event fields, 776 bytes): ncu
+# dram__bytes_{read,write}.sum of all six launches of each kind (three maps
+# of two launch pairs) on the 512 x 512 case, divided by the three maps'
+# steps (3 x 1,463,676,130); the traffic is the stored rows, so it grows
+# with the steps
+DRAM_BYTES_PER_STEP = {
+    0: {"record": (18436688896 + 183303534848) / (3 * 1463676130),
+        "replay": (191494637312 + 1435273472) / (3 * 1463676130)},
+    1: {"record": (10699342336 + 110497920768) / (3 * 1463676130),
+        "replay": (113871344384 + 1407749888) / (3 * 1463676130)},
+}
 
 
 def measured_hbm_peak() -> tuple[float, str]:
@@ -766,7 +772,7 @@ def main():
         roof_replay = None if sp_["replay_fused"] else {"bound": "hbm", "achieved": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9,
                        "peak": hbm_peak, "unit": "GB/s",
                        "frac": rep_bytes / (sp_["replay_replay_ms"] / 1e3) / 1e9 / hbm_peak,
-                       "traffic": REPLAY_DRAM_BYTES_PER_STEP * st["steps"] if REPLAY_DRAM_BYTES_PER_STEP else None,
+                       "traffic": DRAM_BYTES_PER_STEP[int(sp_["replay_split"])]["replay"] * st["steps"],
                        "algorithmic_bytes": rep_bytes, "rows": sp_["replay_rows"],
                        "row_bytes": sp_["replay_row_bytes"],
                        "peak_source": hbm_src,
@@ -805,8 +811,9 @@ def main():
         "wall_ms_per_step_device_loop": 1e3 * wall_dev / args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
                      "frac": achieved_tflops / peak_tflops,
-                     "traffic": (((REC_DRAM_BYTES_PER_STEP + (REPLAY_DRAM_BYTES_PER_STEP if sp_["replay_fused"] else 0))
-                                  * st["steps"] if REC_DRAM_BYTES_PER_STEP else None)
+                     "traffic": ((DRAM_BYTES_PER_STEP[int(sp_["replay_split"])]["record"]
+                                  + (DRAM_BYTES_PER_STEP[int(sp_["replay_split"])]["replay"]
+                                     if sp_["replay_fused"] else 0)) * st["steps"]
                                  if replayed else DRAM_BYTES_PER_MEMBER * n),
                      "traffic_source": "ncu DRAM bytes of the 512 x 512 map, scaled by "
                                        + ("recorded steps" if replayed else "members"),
