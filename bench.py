@@ -723,7 +723,7 @@ def main():
 
     x0_h, pars_h, ts_h = pinned(x0_f), pinned(pars_f), pinned(ts_f)
     F_h = pinned(np.zeros(sim.get_n_features() * n))
-    e2e_times = []
+    e2e_times, e2e_kernel = [], []
     h2d = x0_h.nbytes + pars_h.nbytes + ts_h.nbytes
     d2h = 0
     launches1 = N.lib.clode_launch_count()
@@ -735,6 +735,7 @@ def main():
         sim.features(True)
         F = sim.get_f(out=F_h)
         e2e_times.append(time.perf_counter() - t0)
+        e2e_kernel.append(sim.last_kernel_ms())
         d2h = F.nbytes
     barrier()
     launches_e2e = N.lib.clode_launch_count() - launches1
@@ -825,7 +826,9 @@ def main():
         "roofline_replay": roof_replay,
         "replay": sp_,
         "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * float(np.mean(e2e_times))},
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * float(np.mean(e2e_times)),
+                "ms_all": [round(1e3 * x, 2) for x in e2e_times],
+                "features_device_ms": [round(x, 2) for x in e2e_kernel]},
         "gpu_launches": int(launches_dev + launches_e2e),
         "gpu_launches_detail": {"device_loop": int(launches_dev), "e2e_loop": int(launches_e2e)},
         "clocks": clk,

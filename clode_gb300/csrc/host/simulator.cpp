@@ -1837,41 +1837,41 @@ struct clode_sim {
         schedule = 1;
         ensure_built();
         run_trial();  // untimed: buffers (and the replay's regions) allocated before the timed trials
-        for (auto &cd : cands) {
-            if (maxrregcount != cd[0]) {
-                maxrregcount = cd[0];
+        // register cap and block size for each stepping variant (adaptive
+        // steppers: whole steps or one attempt per iteration; the best cap
+        // differs between them)
+        const bool adaptive = stepper_adaptive();
+        bool best_split = split_attempts;
+        for (int variant = 0; variant < (adaptive ? 2 : 1); ++variant) {
+            const bool sa = adaptive ? variant == 1 : split_attempts;
+            if (sa != split_attempts) {
+                split_attempts = sa;
                 built = false;
             }
-            block_size = cd[1];
-            ensure_built();
-            run_trial();
-            log_msg(CLODE_LOG_INFO, "autotune: maxrregcount=%d block=%d: %.3f ms", cd[0], cd[1], last_ms);
-            if (last_ms < best) {
-                best = last_ms;
-                best_regs = cd[0];
-                best_block = cd[1];
+            for (auto &cd : cands) {
+                if (maxrregcount != cd[0]) {
+                    maxrregcount = cd[0];
+                    built = false;
+                }
+                block_size = cd[1];
+                ensure_built();
+                run_trial();
+                log_msg(CLODE_LOG_INFO, "autotune: split_attempts=%d maxrregcount=%d block=%d: %.3f ms", (int)sa,
+                        cd[0], cd[1], last_ms);
+                if (last_ms < best) {
+                    best = last_ms;
+                    best_regs = cd[0];
+                    best_block = cd[1];
+                    best_split = sa;
+                }
             }
         }
-        if (maxrregcount != best_regs) {
+        if (maxrregcount != best_regs || split_attempts != best_split) {
             maxrregcount = best_regs;
+            split_attempts = best_split;
             built = false;
         }
         block_size = best_block;
-        // the other stepping variant at the best (register cap, block size)
-        if (stepper_adaptive()) {
-            const bool base_split = split_attempts;
-            split_attempts = !base_split;
-            built = false;
-            ensure_built();
-            run_trial();
-            log_msg(CLODE_LOG_INFO, "autotune: split_attempts=%d: %.3f ms", (int)split_attempts, last_ms);
-            if (last_ms < best) {
-                best = last_ms;
-            } else {
-                split_attempts = base_split;
-                built = false;
-            }
-        }
         // replayed or integrated feature pass (two-pass observers, separate passes)
         if (kind == CLODE_SIM_FEATURES && obs_two_pass() && !fuse_init) {
             ensure_built();
