@@ -728,13 +728,19 @@ def main():
     d2h = 0
     launches1 = N.lib.clode_launch_count()
     barrier()
+    parts = np.zeros(4)
     for _ in range(args.steps):
         t0 = time.perf_counter()
         sim.set_problem_data(x0_h, pars_h)
+        t1 = time.perf_counter()
         sim.set_tspan_per_member(ts_h)
+        t2 = time.perf_counter()
         sim.features(True)
+        t3 = time.perf_counter()
         F = sim.get_f(out=F_h)
-        e2e_times.append(time.perf_counter() - t0)
+        t4 = time.perf_counter()
+        e2e_times.append(t4 - t0)
+        parts += np.array([t1 - t0, t2 - t1, t3 - t2, t4 - t3])
         e2e_kernel.append(sim.last_kernel_ms())
         d2h = F.nbytes
     barrier()
@@ -828,7 +834,9 @@ def main():
         "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * float(np.mean(e2e_times)),
                 "ms_all": [round(1e3 * x, 2) for x in e2e_times],
-                "features_device_ms": [round(x, 2) for x in e2e_kernel]},
+                "features_device_ms": [round(x, 2) for x in e2e_kernel],
+                "wall_ms_per_call": dict(zip(("set_problem_data", "set_tspan_per_member", "features", "get_f"),
+                                             (round(1e3 * x / max(args.steps, 1), 2) for x in parts)))},
         "gpu_launches": int(launches_dev + launches_e2e),
         "gpu_launches_detail": {"device_loop": int(launches_dev), "e2e_loop": int(launches_e2e)},
         "clocks": clk,
