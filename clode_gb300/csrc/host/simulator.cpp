@@ -621,6 +621,11 @@ struct clode_sim {
         HostPin(void *ptr, size_t bytes)
         {
             if (ptr && bytes >= ((size_t)32 << 20)) {
+                // memory the caller already page-locked is used as it is
+                cudaPointerAttributes at;
+                if (cudaPointerGetAttributes(&at, ptr) == cudaSuccess && at.type == cudaMemoryTypeHost)
+                    return;
+                (void)cudaGetLastError();
                 if (cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess)
                     p = ptr;
                 else
