@@ -701,6 +701,7 @@ def main():
             stats.append(sim.get_stats())
             split.append({k: sim.get_option(k) for k in ("replay_chunks", "replay_fallback", "replay_rewarm",
                                                           "replay_stages_used", "replay_regions_per_warp",
+                                                          "replay_reallocs",
                                                           "replay_fused", "replay_split",
                                                           "replay_rows", "replay_row_bytes",
                                                           "replay_record_ms", "replay_replay_ms",
@@ -723,7 +724,7 @@ def main():
 
     x0_h, pars_h, ts_h = pinned(x0_f), pinned(pars_f), pinned(ts_f)
     F_h = pinned(np.zeros(sim.get_n_features() * n))
-    e2e_times, e2e_kernel = [], []
+    e2e_times, e2e_kernel, e2e_reallocs, e2e_dl = [], [], [], []
     h2d = x0_h.nbytes + pars_h.nbytes + ts_h.nbytes
     d2h = 0
     launches1 = N.lib.clode_launch_count()
@@ -742,6 +743,8 @@ def main():
         e2e_times.append(t4 - t0)
         parts += np.array([t1 - t0, t2 - t1, t3 - t2, t4 - t3])
         e2e_kernel.append(sim.last_kernel_ms())
+        e2e_reallocs.append(int(sim.get_option("replay_reallocs")))
+        e2e_dl.append([round(sim.get_option(k), 2) for k in ("download_pin_ms", "download_ms", "download_wall_ms")])
         d2h = F.nbytes
     barrier()
     launches_e2e = N.lib.clode_launch_count() - launches1
@@ -835,6 +838,8 @@ def main():
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * float(np.mean(e2e_times)),
                 "ms_all": [round(1e3 * x, 2) for x in e2e_times],
                 "features_device_ms": [round(x, 2) for x in e2e_kernel],
+                "replay_reallocs": e2e_reallocs,
+                "get_f_pin_device_wall_ms": e2e_dl,
                 "wall_ms_per_call": dict(zip(("set_problem_data", "set_tspan_per_member", "features", "get_f"),
                                              (round(1e3 * x / max(args.steps, 1), 2) for x in parts)))},
         "gpu_launches": int(launches_dev + launches_e2e),

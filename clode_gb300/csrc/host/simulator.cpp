@@ -275,6 +275,7 @@ struct clode_sim {
     unsigned int last_regions_per_warp = 0;  // regions each replay warp of the last replayed run took
     unsigned int last_rewarm = 0;          // of last_fallback: members whose warm-up was run again
     double last_rows = 0.0;                // rows the last replayed run recorded (all regions, all launches)
+    unsigned int last_reallocs = 0;        // record-region allocations the last replayed run made
     double last_warmup_ms = 0.0;           // the separate warm-up launch of the last integrated features run
     double replay_steps_per_member = 0.0;  // measured by the last replayed run (sizes the next one)
     int last_replay_chunks = 0;            // recording launches of the last replayed run
@@ -307,6 +308,9 @@ struct clode_sim {
             if (ev1)
                 cudaEventDestroy(ev1);
             for (cudaEvent_t &e : rev)
+                if (e)
+                    cudaEventDestroy(e);
+            for (cudaEvent_t &e : dl_ev)
                 if (e)
                     cudaEventDestroy(e);
         }
@@ -645,7 +649,13 @@ struct clode_sim {
     {
         if (n == 0)
             return;
+        const auto w0 = std::chrono::steady_clock::now();
         HostPin pin(dst, n * sizeof(double));
+        const auto w1 = std::chrono::steady_clock::now();
+        for (cudaEvent_t *e : {&dl_ev[0], &dl_ev[1]})
+            if (!*e)
+                check_cuda(cudaEventCreate(e), "cudaEventCreate");
+        check_cuda(cudaEventRecord(dl_ev[0], stream), "event record");
         if (single) {
             stage.reserve(n * sizeof(double));
             launch_f32_to_f64(src.as<float>(), stage.as<double>(), n, stream);
@@ -653,8 +663,16 @@ struct clode_sim {
         } else {
             check_cuda(cudaMemcpyAsync(dst, src.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H copy");
         }
+        check_cuda(cudaEventRecord(dl_ev[1], stream), "event record");
         check_cuda(cudaStreamSynchronize(stream), "D2H copy");
+        float ms = 0.0f;
+        check_cuda(cudaEventElapsedTime(&ms, dl_ev[0], dl_ev[1]), "event timing");
+        last_download_ms = ms;
+        last_download_pin_ms = std::chrono::duration<double, std::milli>(w1 - w0).count();
+        last_download_wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
     }
+    cudaEvent_t dl_ev[2] = {nullptr, nullptr};
+    double last_download_ms = 0.0, last_download_wall_ms = 0.0, last_download_pin_ms = 0.0;
 
     void fill_real(DevBuf &b, double v, size_t n)
     {
@@ -1112,6 +1130,16 @@ struct clode_sim {
     bool replay_regions(double budget, unsigned long long warps, double row_bytes, size_t rs,
                         unsigned long long &rows, unsigned int &members_cap)
     {
+        // regions already allocated that hold at least nine tenths of the
+        // budget's rows are used as they are: freeing and re-allocating a
+        // few hundred GB costs more (the next transfers wait for the unmap)
+        // than the rows it would add
+        if (rec.p && warps > 0) {
+            const double held_rows = (double)rec.bytes / ((double)warps * (double)rec_fields * 32.0 * (double)rs);
+            const double want_rows = budget / ((double)warps * (row_bytes + 0.5));
+            if (want_rows > held_rows && want_rows <= 1.1 * held_rows)
+                budget = held_rows * (double)warps * (row_bytes + 0.5);
+        }
         rows = (unsigned long long)(budget / ((double)warps * (row_bytes + 0.5)));
         // a multiple of 16 rows: every region's masks start on a 16-byte
         // boundary, as the replay's bulk L2 prefetches require
@@ -1119,6 +1147,8 @@ struct clode_sim {
         if (rows < 64)
             return false;
         members_cap = (unsigned int)std::min<unsigned long long>(rows / 8 + 64, 0x7fffffffull);
+        if (rec.bytes < (size_t)(warps * rows * rec_fields * 32ull * rs))
+            ++last_reallocs;
         rec.reserve((size_t)(warps * rows * rec_fields * 32ull * rs));
         rec_mask.reserve((size_t)(warps * rows * 2ull * sizeof(unsigned int)) + 16);
         rec_member.reserve((size_t)(warps * members_cap * sizeof(int)));
@@ -1202,6 +1232,7 @@ struct clode_sim {
     bool replay_run(long long positions)
     {
         const bool fused = replay_fused && kp_record_replay;
+        last_reallocs = 0;
         unsigned int grid = 0, block = 0;
         persistent_shape(fused ? kp_record_replay : kp_init_rec, positions, grid, block);
         const unsigned long long warps = (unsigned long long)grid * block / 32;
@@ -2714,6 +2745,10 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "replay_regions_per_warp") *value = sim->last_regions_per_warp;
         else if (k == "replay_rewarm") *value = sim->last_rewarm;
         else if (k == "replay_rows") *value = sim->last_rows;
+        else if (k == "replay_reallocs") *value = sim->last_reallocs;
+        else if (k == "download_ms") *value = sim->last_download_ms;
+        else if (k == "download_wall_ms") *value = sim->last_download_wall_ms;
+        else if (k == "download_pin_ms") *value = sim->last_download_pin_ms;
         else if (k == "replay_row_bytes")  // one warp-wide row: every stored field of 32 lanes and the two masks
             *value = sim->rec_fields ? (double)sim->rec_fields * 32.0 * (double)sim->real_size() + 8.0 : 0.0;
         else if (k == "warmup_ms") *value = sim->last_warmup_ms;

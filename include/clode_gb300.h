@@ -338,7 +338,11 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * recorded), "replay_row_bytes" (bytes of one warp-wide row of the built
  * program), "replay_stages_used", "replay_regions_per_warp" (regions each
  * replay warp took: more than one when the replay's blocks fit on an SM
- * fewer at a time than the recording launch's), "warmup_ms" (the separate warm-up launch
+ * fewer at a time than the recording launch's), "replay_reallocs" (record
+ * region allocations the last replayed run made), "download_ms",
+ * "download_wall_ms", "download_pin_ms" (the last device-to-host transfer of
+ * a getter: device time of its conversion and copy, wall time, time spent
+ * page-locking the destination), "warmup_ms" (the separate warm-up launch
  * of the last integrated features run),
  * "replay_record_ms", "replay_replay_ms", "replay_fallback_ms" (device time
  * of each launch kind).
