@@ -652,27 +652,32 @@ struct clode_sim {
         const auto w0 = std::chrono::steady_clock::now();
         HostPin pin(dst, n * sizeof(double));
         const auto w1 = std::chrono::steady_clock::now();
-        for (cudaEvent_t *e : {&dl_ev[0], &dl_ev[1]})
+        for (cudaEvent_t *e : {&dl_ev[0], &dl_ev[1], &dl_ev[2]})
             if (!*e)
                 check_cuda(cudaEventCreate(e), "cudaEventCreate");
         check_cuda(cudaEventRecord(dl_ev[0], stream), "event record");
+        check_cuda(cudaEventRecord(dl_ev[2], stream), "event record");
         if (single) {
             stage.reserve(n * sizeof(double));
             launch_f32_to_f64(src.as<float>(), stage.as<double>(), n, stream);
+            check_cuda(cudaEventRecord(dl_ev[2], stream), "event record");
             check_cuda(cudaMemcpyAsync(dst, stage.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H copy");
         } else {
             check_cuda(cudaMemcpyAsync(dst, src.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H copy");
         }
         check_cuda(cudaEventRecord(dl_ev[1], stream), "event record");
         check_cuda(cudaStreamSynchronize(stream), "D2H copy");
-        float ms = 0.0f;
+        float ms = 0.0f, cv = 0.0f;
         check_cuda(cudaEventElapsedTime(&ms, dl_ev[0], dl_ev[1]), "event timing");
+        check_cuda(cudaEventElapsedTime(&cv, dl_ev[0], dl_ev[2]), "event timing");
         last_download_ms = ms;
+        last_download_convert_ms = cv;
         last_download_pin_ms = std::chrono::duration<double, std::milli>(w1 - w0).count();
         last_download_wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
     }
-    cudaEvent_t dl_ev[2] = {nullptr, nullptr};
+    cudaEvent_t dl_ev[3] = {nullptr, nullptr, nullptr};
     double last_download_ms = 0.0, last_download_wall_ms = 0.0, last_download_pin_ms = 0.0;
+    double last_download_convert_ms = 0.0;
 
     void fill_real(DevBuf &b, double v, size_t n)
     {
@@ -2749,6 +2754,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "download_ms") *value = sim->last_download_ms;
         else if (k == "download_wall_ms") *value = sim->last_download_wall_ms;
         else if (k == "download_pin_ms") *value = sim->last_download_pin_ms;
+        else if (k == "download_convert_ms") *value = sim->last_download_convert_ms;
         else if (k == "replay_row_bytes")  // one warp-wide row: every stored field of 32 lanes and the two masks
             *value = sim->rec_fields ? (double)sim->rec_fields * 32.0 * (double)sim->real_size() + 8.0 : 0.0;
         else if (k == "warmup_ms") *value = sim->last_warmup_ms;

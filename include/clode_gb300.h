@@ -340,9 +340,10 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * replay warp took: more than one when the replay's blocks fit on an SM
  * fewer at a time than the recording launch's), "replay_reallocs" (record
  * region allocations the last replayed run made), "download_ms",
- * "download_wall_ms", "download_pin_ms" (the last device-to-host transfer of
- * a getter: device time of its conversion and copy, wall time, time spent
- * page-locking the destination), "warmup_ms" (the separate warm-up launch
+ * "download_wall_ms", "download_pin_ms", "download_convert_ms" (the last
+ * device-to-host transfer of a getter: device time of its conversion and
+ * copy, wall time, time spent page-locking the destination, device time of
+ * the conversion alone), "warmup_ms" (the separate warm-up launch
  * of the last integrated features run),
  * "replay_record_ms", "replay_replay_ms", "replay_fallback_ms" (device time
  * of each launch kind).
