@@ -601,10 +601,31 @@ struct clode_sim {
     }
 
     // ---------------------------------------------------- problem data --
+    // The device address of page-locked host memory the caller holds (null
+    // for any other memory): kernels read and write it directly, over the
+    // host link, without a staging copy.
+    static void *pinned_device_ptr(const void *host)
+    {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return nullptr;
+        }
+        return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+    }
+
     void upload(DevBuf &dst, const double *src, size_t n)
     {
         if (n == 0)
             return;
+        if (single) {
+            // page-locked source: converted straight from host memory
+            if (void *d = pinned_device_ptr(src)) {
+                launch_f64_to_f32(static_cast<const double *>(d), dst.as<float>(), n, stream);
+                check_cuda(cudaStreamSynchronize(stream), "H2D conversion");
+                return;
+            }
+        }
         HostPin pin(const_cast<double *>(src), n * sizeof(double));
         if (single) {
             stage.reserve(n * sizeof(double));
@@ -650,14 +671,19 @@ struct clode_sim {
         if (n == 0)
             return;
         const auto w0 = std::chrono::steady_clock::now();
-        HostPin pin(dst, n * sizeof(double));
+        // page-locked destination: the conversion kernel writes it directly
+        void *direct = single ? pinned_device_ptr(dst) : nullptr;
+        HostPin pin(direct ? nullptr : dst, n * sizeof(double));
         const auto w1 = std::chrono::steady_clock::now();
         for (cudaEvent_t *e : {&dl_ev[0], &dl_ev[1], &dl_ev[2]})
             if (!*e)
                 check_cuda(cudaEventCreate(e), "cudaEventCreate");
         check_cuda(cudaEventRecord(dl_ev[0], stream), "event record");
         check_cuda(cudaEventRecord(dl_ev[2], stream), "event record");
-        if (single) {
+        if (direct) {
+            launch_f32_to_f64(src.as<float>(), static_cast<double *>(direct), n, stream);
+            check_cuda(cudaEventRecord(dl_ev[2], stream), "event record");
+        } else if (single) {
             stage.reserve(n * sizeof(double));
             launch_f32_to_f64(src.as<float>(), stage.as<double>(), n, stream);
             check_cuda(cudaEventRecord(dl_ev[2], stream), "event record");

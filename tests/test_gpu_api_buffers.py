@@ -1,7 +1,9 @@
 """Getters into a caller's buffer (``get_f(out=...)``, no reference
 counterpart): the values equal those of the allocating getter, the buffer
 may be larger than needed and may be page-locked host memory reused between
-calls; a buffer of the wrong type or size is refused."""
+calls (which the conversion kernel writes directly); a buffer of the wrong
+type or size is refused.  Inputs in page-locked host memory (read directly
+by the conversion kernel) give the results of ordinary arrays."""
 import numpy as np
 import pytest
 
@@ -47,3 +49,26 @@ def test_get_f_refuses_unfit_buffers():
     for bad in (np.zeros(n - 1), np.zeros(n, dtype=np.float32), np.zeros((n, 2))[:, 0]):
         with pytest.raises(ValueError):
             sim.get_f(out=bad)
+
+
+def test_page_locked_inputs_give_the_same_results():
+    torch = pytest.importorskip("torch")
+    n = 3000
+    r = np.random.default_rng(1)
+    x0 = (np.ones((n, 3)) + r.normal(0, 1e-3, (n, 3))).flatten(order="F")
+    pars = np.stack([r.uniform(10, 40, n), r.uniform(5, 15, n), np.full(n, 8 / 3)], axis=1).flatten(order="F")
+
+    def pinned(a):
+        b = torch.empty(a.size, dtype=torch.float64, pin_memory=True).numpy()
+        b[:] = a
+        return b
+
+    outs = []
+    for x, p in ((x0, pars), (pinned(x0), pinned(pars))):
+        sim = _sim(10)
+        sim.set_problem_data(x, p)
+        sim.set_tspan([0.0, 20.0])
+        sim.features(True)
+        outs.append((sim.get_f(), np.asarray(sim.get_x0()), np.asarray(sim.get_pars())))
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b, equal_nan=True)
