@@ -592,6 +592,8 @@ def main():
     ap.add_argument("--replay-split", type=int, default=None,
                     help="replay rows of the observer's event fields with the pass's sums taken while recording "
                          "(1, the engine default) or whole rows (0)")
+    ap.add_argument("--replay-room", type=float, default=None,
+                    help="region room kept for the members in flight, in mean member lengths (engine default 2.5)")
     ap.add_argument("--replay-fused", type=int, default=None,
                     help="recording and replay in one launch per launch pair (1) or two launches (0)")
     ap.add_argument("--replay-stages", type=int, default=None,
@@ -657,7 +659,8 @@ def main():
                      ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm),
                      ("order_by_span", args.order_by_span), ("replay", args.replay), ("replay_mb", args.replay_mb),
                      ("precise", args.precise), ("replay_stages", args.replay_stages),
-                     ("replay_split", args.replay_split), ("replay_fused", args.replay_fused)):
+                     ("replay_split", args.replay_split), ("replay_fused", args.replay_fused),
+                     ("replay_room", args.replay_room)):
         if val is not None:
             sim.set_option(key, val)
     sim.build_cl()

@@ -264,6 +264,7 @@ struct clode_sim {
                                 // -1: up to 4 that fit)
     double replay_cap_scale = 1.0;  // autotuner trials on a sample: the regions' memory scaled by its fraction
     bool replay_split = false;  // rows of the observer's event fields, the pass's sums taken while recording
+    double replay_room = 2.5;   // region room kept for the members in flight, in mean member lengths
     bool replay_fused = false;  // recording and replay in one launch per launch pair
     bool predraw = false;       // stochastic trajectories: deviates drawn by their own launches first
     bool noise_on = false;      // make_args: the launch reads the pre-drawn deviates
@@ -1313,12 +1314,14 @@ struct clode_sim {
         if (!fused)
             replay_shape(grid, block, (unsigned int)(rec_fields * 32u * rs), per_warp, rblock, stages, stage_smem);
         // a warp takes no new member once its region is this full: the members
-        // it holds then must still fit (2.5 times the average member's steps)
+        // it holds then should still fit (replay_room times the average
+        // member's steps); a larger room makes longer drains, a smaller one
+        // more members cut off by a full region (run again by the plain passes)
         double spm = replay_steps_per_member;
         auto fetch_rows_for = [&](unsigned long long rows) {
             unsigned long long room = rows / 2;
             if (spm > 0.0)
-                room = std::min<unsigned long long>(room, (unsigned long long)(2.5 * spm) + 64);
+                room = std::min<unsigned long long>(room, (unsigned long long)(replay_room * spm) + 64);
             return rows - room;
         };
 
@@ -2725,6 +2728,10 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 sim->noise.release();
                 sim->noise_count.release();
             }
+        } else if (k == "replay_room") {
+            if (!(value >= 0.0 && value <= 100.0))
+                fail(CLODE_ERR_INVALID_ARGUMENT, "replay_room must be in [0, 100]");
+            sim->replay_room = value;
         } else if (k == "replay_fused") {
             sim->replay_fused = value != 0.0;
         } else if (k == "replay_stages") {
@@ -2769,6 +2776,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "replay_stages") *value = sim->replay_stages;
         else if (k == "replay_split") *value = sim->replay_split;
         else if (k == "replay_fused") *value = sim->replay_fused;
+        else if (k == "replay_room") *value = sim->replay_room;
         else if (k == "predraw") *value = sim->predraw;
         else if (k == "predrawn") *value = sim->last_predrawn;
         else if (k == "predraw_ms") *value = sim->last_draw_ms;
