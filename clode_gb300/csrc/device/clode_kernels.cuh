@@ -1036,10 +1036,18 @@ __device__ __forceinline__ void record_body(const Args &a)
     Counters c = {0, 0, 0, 0};
     const unsigned int lane = threadIdx.x & 31u;
     const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long R = a.rec_rows;
-    unsigned long long row = 0;  // warp-uniform
-    unsigned int starts = 0;     // warp-uniform: members started in this region
-    bool full = false;           // warp-uniform: the region has no row left
+    // a region's rows fit 32 bits (the host keeps rec_rows below 2^32)
+    const unsigned int R = (unsigned int)a.rec_rows;
+    const unsigned int fetch_rows = (unsigned int)(a.rec_fetch_rows < a.rec_rows ? a.rec_fetch_rows : a.rec_rows);
+    // this lane's column of the current row, advanced one row per iteration
+    realtype *col = a.rec + warp * R * (CLODE_REC_FIELDS * 32ull) + lane;
+    // the region's masks, stored 32 rows at a time: lane k holds row k's of
+    // the current group of 32 (valid lanes, lanes that start a member)
+    uint2 *const masks = reinterpret_cast<uint2 *>(a.rec_mask + 2ull * warp * R);
+    unsigned int mv = 0u, ms = 0u;
+    unsigned int row = 0;     // warp-uniform
+    unsigned int starts = 0;  // warp-uniform: members started in this region
+    bool full = false;        // warp-uniform: the region has no row left
     bool exhausted = false;
     int i = -1;
     bool fresh = false, tail = false, first = false, hmin_fail = false;
@@ -1053,7 +1061,7 @@ __device__ __forceinline__ void record_body(const Args &a)
     StepCtl sc;
     sc.retry = false;
     for (;;) {
-        const bool want = i < 0 && !exhausted && row < a.rec_fetch_rows && starts + 32u <= a.rec_members;
+        const bool want = i < 0 && !exhausted && row < fetch_rows && starts + 32u <= a.rec_members;
         const int got = fetch_member(a, want);
         if (want) {
             if (got < 0) {
@@ -1110,9 +1118,8 @@ __device__ __forceinline__ void record_body(const Args &a)
             {
                 const unsigned int vmask = __ballot_sync(0xffffffffu, valid);
                 const unsigned int smask = __ballot_sync(0xffffffffu, valid && first);
-                const unsigned long long cell = warp * R + row;
                 if (valid) {
-                    realtype *r = a.rec + cell * (CLODE_REC_FIELDS * 32ull) + lane;
+                    realtype *r = col;
 #if defined(CLODE_OBS_SPLIT)
                     Observer::rec_store(r, m.t, m.x, m.dx, m.aux, a.op);
                     fs.update(m.t, m.x, m.dx, m.aux);
@@ -1134,12 +1141,15 @@ __device__ __forceinline__ void record_body(const Args &a)
                         first = false;
                     }
                 }
-                if (lane == 0) {
-                    a.rec_mask[2 * cell] = vmask;
-                    a.rec_mask[2 * cell + 1] = smask;
+                if (lane == (row & 31u)) {
+                    mv = vmask;
+                    ms = smask;
                 }
+                if ((row & 31u) == 31u)
+                    masks[row - 31u + lane] = make_uint2(mv, ms);
                 starts += __popc(smask);
                 ++row;
+                col += CLODE_REC_FIELDS * 32;
             }
         }
         if (i >= 0 && !running) {
@@ -1186,8 +1196,11 @@ __device__ __forceinline__ void record_body(const Args &a)
             break;
         }
     }
+    // the masks of the last, partial group of 32 rows
+    if (lane < (row & 31u))
+        masks[(row & ~31u) + lane] = make_uint2(mv, ms);
     if (lane == 0)
-        a.rec_used[warp] = (unsigned int)(row < R ? row : R);
+        a.rec_used[warp] = row < R ? row : R;
     flush_counters(a, c);
 }
 
