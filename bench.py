@@ -580,6 +580,8 @@ def main():
     ap.add_argument("--ftz", type=int, default=1)
     ap.add_argument("--fast-math", type=int, default=0, help="approximate exp/pow/sqrt (NVRTC --use_fast_math)")
     ap.add_argument("--fast-exp", type=int, default=0, help="the model's FP32 exp within 2.5 ulp (own Cody-Waite exp)")
+    ap.add_argument("--paired", type=int, default=None,
+                    help="FP32 stage sums two variables per paired instruction (engine default 1)")
     ap.add_argument("--maxrreg", type=int, default=None)
     ap.add_argument("--blocks-per-sm", type=int, default=None)
     ap.add_argument("--split-attempts", type=int, default=None)
@@ -654,7 +656,7 @@ def main():
     sim.set_option("schedule", args.schedule)
     sim.set_option("block_size", args.block_size)
     for key, val in (("prec_div", args.prec_div), ("ftz", args.ftz), ("fast_math", args.fast_math),
-                     ("fast_exp", args.fast_exp), ("split_attempts", args.split_attempts),
+                     ("fast_exp", args.fast_exp), ("paired", args.paired), ("split_attempts", args.split_attempts),
                      ("fuse_init", args.fuse_init), ("step_block", args.step_block),
                      ("maxrregcount", args.maxrreg), ("blocks_per_sm", args.blocks_per_sm),
                      ("order_by_span", args.order_by_span), ("replay", args.replay), ("replay_mb", args.replay_mb),
@@ -811,6 +813,7 @@ def main():
                    "block_size": args.block_size, "fmad": bool(args.fmad),
                    "variant": {k: v for k, v in (("prec_div", args.prec_div), ("ftz", args.ftz),
                                                  ("fast_math", args.fast_math), ("fast_exp", args.fast_exp),
+                                                 ("paired", args.paired),
                                                  ("maxrregcount", args.maxrreg),
                                                  ("blocks_per_sm", args.blocks_per_sm)) if v is not None},
                    "registers": sim.kernel_registers("features_persistent" if sim.get_option("schedule") else "features"),
@@ -880,7 +883,7 @@ def main():
         # the engine's precise option (FP32 integration, compensated sums,
         # event times refined in FP64) on the same members and build options
         ps = W.FeatureSimulatorBase(pi, "dopri5", "nhood2", op, True, res, "")
-        for key in ("fmad", "prec_div", "ftz", "fast_math", "fast_exp", "maxrregcount", "split_attempts",
+        for key in ("fmad", "prec_div", "ftz", "fast_math", "fast_exp", "paired", "maxrregcount", "split_attempts",
                     "schedule", "block_size"):
             ps.set_option(key, sim.get_option(key))
         ps.set_option("precise", 1)
@@ -895,7 +898,7 @@ def main():
         line["error_vs_fp64"] = {"reference_run": "CPU oracle, FP64, DP45 rtol = abstol = 1e-10, same members",
                                  "gpu_fp32": _vs64(Fg), "gpu_fp32_precise": _vs64(Fq), "cpu_fp32": _vs64(Fc)}
     opts = {k: sim.get_option(k) for k in ("schedule", "block_size", "maxrregcount", "fmad", "prec_div", "ftz",
-                                           "fast_math", "fast_exp", "split_attempts", "fuse_init")}
+                                           "fast_math", "fast_exp", "paired", "split_attempts", "fuse_init")}
     # the map's simulator (and the device memory of its stored steps) is not
     # needed by the workloads below
     del sim

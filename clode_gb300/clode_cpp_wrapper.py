@@ -647,7 +647,8 @@ class SimulatorBase:
 
     def autotune(self, sample: int = 0) -> dict:
         """Pick register cap, block size, (adaptive steppers) the stepping
-        variant and (two-pass observers) the replayed or integrated feature
+        variant, (FP32 Dormand-Prince builds with contraction) paired or scalar
+        stage sums and (two-pass observers) the replayed or integrated feature
         pass (and the replay's row and launch layout) and fused or separate
         observer initialisation, by timing the
         persistent kernels on a strided sample of ``sample`` members (no
@@ -657,6 +658,7 @@ class SimulatorBase:
         return {"ms": ms.value, "maxrregcount": int(self.get_option("maxrregcount")),
                 "block_size": int(self.get_option("block_size")),
                 "split_attempts": int(self.get_option("split_attempts")),
+                "paired": int(self.get_option("paired")),
                 "fuse_init": int(self.get_option("fuse_init")), "replay": int(self.get_option("replay")),
                 "replay_split": int(self.get_option("replay_split")),
                 "replay_fused": int(self.get_option("replay_fused"))}

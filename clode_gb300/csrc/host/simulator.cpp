@@ -245,6 +245,7 @@ struct clode_sim {
     bool ftz = false;
     bool fast_math = false;
     bool fast_exp = false;        // FP32 exp and controller pow of a few ulp (CLODE_FAST_EXP)
+    bool paired = true;           // FP32 Runge-Kutta stages two variables per instruction (CLODE_PAIRED)
     bool precise = false;         // precision option (CLODE_PRECISE): compensated time and means,
                                   // compensated error estimate, refined event times
     bool split_attempts = false;  // persistent kernels: one adaptive attempt per loop iteration
@@ -328,6 +329,8 @@ struct clode_sim {
 
     size_t real_size() const { return single ? sizeof(float) : sizeof(double); }
     bool stepper_adaptive() const { return stepper == "bs23" || stepper == "dopri5"; }
+    // the builds in which the option "paired" changes the program (CLODE_PAIRED_STAGES)
+    bool pairing_applies() const { return single && fmad && stepper == "dopri5" && nVar >= 2 && !precise; }
     bool obs_two_pass() const { return observer == "thresh2" || observer == "nhood2"; }
 
     // --------------------------------------------------------- set-up --
@@ -485,6 +488,9 @@ struct clode_sim {
                      "-DN_AUX=" + std::to_string(nAux), "-DN_WIENER=" + std::to_string(nWiener),
                      std::string("-DCLODE_SPLIT_ATTEMPTS=") + (split_attempts ? "1" : "0"),
                      std::string("-DCLODE_FAST_EXP=") + (fast_exp ? "1" : "0"),
+                     std::string("-DCLODE_PAIRED=") + (paired ? "1" : "0"),
+                     std::string("-DCLODE_FMAD=") + (fmad ? "1" : "0"),
+                     std::string("-DCLODE_FTZ=") + (ftz || fast_math ? "1" : "0"),
                      std::string("-DCLODE_PRECISE=") + (precise ? "1" : "0"),
                      "-DCLODE_STEP_BLOCK=" + std::to_string(step_block)};
         if (kind == CLODE_SIM_FEATURES) {
@@ -1908,37 +1914,51 @@ struct clode_sim {
         ensure_built();
         run_trial();  // untimed: buffers (and the replay's regions) allocated before the timed trials
         // register cap and block size for each stepping variant (adaptive
-        // steppers: whole steps or one attempt per iteration; the best cap
-        // differs between them)
+        // steppers: whole steps or one attempt per iteration) and, where they
+        // apply (FP32 Dormand-Prince builds with contraction), paired or
+        // scalar stage sums: the best cap differs between them, and whether
+        // pairing pays depends on the model (it costs register moves and
+        // longer dependent chains that a cheap right-hand side does not hide)
         const bool adaptive = stepper_adaptive();
         bool best_split = split_attempts;
-        for (int variant = 0; variant < (adaptive ? 2 : 1); ++variant) {
-            const bool sa = adaptive ? variant == 1 : split_attempts;
-            if (sa != split_attempts) {
-                split_attempts = sa;
+        bool best_paired = paired;
+        const bool pair_choice = pairing_applies();
+        for (int pv = 0; pv < (pair_choice ? 2 : 1); ++pv) {
+            const bool pd = pair_choice ? pv == 0 : paired;
+            if (pd != paired) {
+                paired = pd;
                 built = false;
             }
-            for (auto &cd : cands) {
-                if (maxrregcount != cd[0]) {
-                    maxrregcount = cd[0];
+            for (int variant = 0; variant < (adaptive ? 2 : 1); ++variant) {
+                const bool sa = adaptive ? variant == 1 : split_attempts;
+                if (sa != split_attempts) {
+                    split_attempts = sa;
                     built = false;
                 }
-                block_size = cd[1];
-                ensure_built();
-                run_trial();
-                log_msg(CLODE_LOG_INFO, "autotune: split_attempts=%d maxrregcount=%d block=%d: %.3f ms", (int)sa,
-                        cd[0], cd[1], last_ms);
-                if (last_ms < best) {
-                    best = last_ms;
-                    best_regs = cd[0];
-                    best_block = cd[1];
-                    best_split = sa;
+                for (auto &cd : cands) {
+                    if (maxrregcount != cd[0]) {
+                        maxrregcount = cd[0];
+                        built = false;
+                    }
+                    block_size = cd[1];
+                    ensure_built();
+                    run_trial();
+                    log_msg(CLODE_LOG_INFO, "autotune: paired=%d split_attempts=%d maxrregcount=%d block=%d: %.3f ms",
+                            (int)pd, (int)sa, cd[0], cd[1], last_ms);
+                    if (last_ms < best) {
+                        best = last_ms;
+                        best_regs = cd[0];
+                        best_block = cd[1];
+                        best_split = sa;
+                        best_paired = pd;
+                    }
                 }
             }
         }
-        if (maxrregcount != best_regs || split_attempts != best_split) {
+        if (maxrregcount != best_regs || split_attempts != best_split || paired != best_paired) {
             maxrregcount = best_regs;
             split_attempts = best_split;
+            paired = best_paired;
             built = false;
         }
         block_size = best_block;
@@ -2667,12 +2687,14 @@ int clode_sim_set_option(clode_sim *sim, const char *key, double value)
                 sim->fmad = v;
                 sim->built = false;
             }
-        } else if (k == "prec_div" || k == "ftz" || k == "fast_math" || k == "fast_exp" || k == "split_attempts") {
+        } else if (k == "prec_div" || k == "ftz" || k == "fast_math" || k == "fast_exp" || k == "paired" ||
+                   k == "split_attempts") {
             bool v = value != 0.0;
             bool &field = k == "prec_div"    ? sim->prec_div
                           : k == "ftz"       ? sim->ftz
                           : k == "fast_math" ? sim->fast_math
                           : k == "fast_exp"  ? sim->fast_exp
+                          : k == "paired"    ? sim->paired
                                              : sim->split_attempts;
             if (v != field) {
                 field = v;
@@ -2762,6 +2784,7 @@ int clode_sim_get_option(clode_sim *sim, const char *key, double *value)
         else if (k == "ftz") *value = sim->ftz;
         else if (k == "fast_math") *value = sim->fast_math;
         else if (k == "fast_exp") *value = sim->fast_exp;
+        else if (k == "paired") *value = sim->paired;
         else if (k == "split_attempts") *value = sim->split_attempts;
         else if (k == "step_block") *value = sim->step_block;
         else if (k == "maxrregcount") *value = sim->maxrregcount;

@@ -290,6 +290,9 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * "fast_math" (1: approximate exp/log/pow/sin/cos/sqrt, implies prec_div 0 and ftz 1),
  * "fast_exp" (1: the model's FP32 exp within 2.5 ulp by Cody-Waite splitting and the
  * hardware exp2; the step-size controller keeps pow),
+ * "paired" (1, the default: FP32 Dormand-Prince stage sums take two state
+ * variables per paired FP32 instruction; with fmad 0 the results are bitwise those
+ * of paired 0; with fmad 1 the contraction pattern is fixed by the engine),
  * "maxrregcount" (0: no cap, else 32..255 registers per thread),
  * "split_attempts" (adaptive steppers, persistent kernels: 1 = one step attempt per
  * loop iteration, a rejected attempt retried in the next; results are identical),
@@ -347,8 +350,8 @@ int clode_sim_last_kernel_ms(clode_sim *sim, double *ms);
  * of the last integrated features run),
  * "replay_record_ms", "replay_replay_ms", "replay_fallback_ms" (device time
  * of each launch kind).
- * Changing a build option (fmad, prec_div, ftz, fast_math, fast_exp, maxrregcount,
- * split_attempts, step_block, precise) recompiles the program at the next run. */
+ * Changing a build option (fmad, prec_div, ftz, fast_math, fast_exp, paired,
+ * maxrregcount, split_attempts, step_block, precise) recompiles the program at the next run. */
 int clode_sim_set_option(clode_sim *sim, const char *key, double value);
 int clode_sim_get_option(clode_sim *sim, const char *key, double *value);
 /* Chains: ops run back to back on the simulator's stream, one synchronisation
@@ -361,10 +364,13 @@ int clode_sim_chain(clode_sim *sim, const int *ops, int n_ops, int use_graph);
 /* Autotuner: times the persistent kernel of this simulator's kind on members
  * [0, sample) (sample <= 0: all) for register caps {none, 128, 96, 80, 64} and
  * block sizes {64, 128}, keeps the fastest ("maxrregcount", "block_size",
- * schedule 1), then for adaptive steppers also times the other value of the
- * "split_attempts" option at that pair and keeps the faster, for two-pass
- * observers (nhood2, thresh2) also the other value of "fuse_init", and
- * returns the best time.  Numerics options are not changed.  The sampled members' dt and
+ * schedule 1) for each value of "split_attempts" (adaptive steppers) and, in
+ * FP32 Dormand-Prince builds with fmad 1, of "paired"; keeps the fastest; for
+ * two-pass observers (nhood2, thresh2) also times the other values of the replay
+ * options and of "fuse_init"; returns the best time.  Numerics options (fmad,
+ * prec_div, ftz, fast_math, fast_exp, precise) are not changed; with fmad 1 the
+ * choice of "paired" changes how the stage sums are rounded, with fmad 0 nothing
+ * it chooses changes a result bit.  The sampled members' dt and
  * RNG state are restored; the observer is re-initialised at the next
  * features run. */
 int clode_sim_autotune(clode_sim *sim, long long sample, double *best_ms);
