@@ -52,6 +52,24 @@ __device__ __forceinline__ realtype mean_time(realtype mean, realtype v, realtyp
     return mean + (v - mean) * dt / elapsed;
 }
 
+// Builds with approximate division (prec_div 0: CLODE_PREC_DIV = 0) take the
+// step's time weight dt / elapsed once for all of a step's time-weighted
+// means, and divide the neighbourhood test's distances by per-member
+// reciprocals of the ranges: the same quotients within the approximate
+// division's own error, with one division per step instead of one per
+// variable.  Builds with IEEE division (the default, and the build that
+// reproduces the reference) divide per variable as the reference does.
+#ifndef CLODE_PREC_DIV
+#define CLODE_PREC_DIV 1
+#endif
+#define CLODE_SHARED_DIV (!CLODE_PREC_DIV && !CLODE_PRECISE)
+#if CLODE_SHARED_DIV
+__device__ __forceinline__ realtype mean_weighted(realtype mean, realtype v, realtype w)
+{
+    return mean + (v - mean) * w;
+}
+#endif
+
 __device__ __forceinline__ void mean_count(realtype &mean, realtype v, unsigned int n)
 {
     if (n == 1)
@@ -242,6 +260,9 @@ struct Extent {
     __device__ __forceinline__ void update(const realtype (&x)[N_VAR], const realtype (&dx)[N_VAR],
                                            const realtype (&aux)[NA1], realtype dt, realtype elapsed)
     {
+#if CLODE_SHARED_DIV
+        const realtype w = dt / elapsed;
+#endif
 #pragma unroll
         for (int j = 0; j < N_VAR; ++j) {
             xmax[j] = fmax(x[j], xmax[j]);
@@ -251,6 +272,8 @@ struct Extent {
             cs.add_prod(x[j], dt);
             xmean[j] = cs.hi;
             xlo[j] = cs.lo;
+#elif CLODE_SHARED_DIV
+            xmean[j] = mean_weighted(xmean[j], x[j], w);
 #else
             xmean[j] = mean_time(xmean[j], x[j], dt, elapsed);
 #endif
@@ -266,6 +289,8 @@ struct Extent {
             cs.add_prod(aux[j], dt);
             amean[j] = cs.hi;
             alo[j] = cs.lo;
+#elif CLODE_SHARED_DIV
+            amean[j] = mean_weighted(amean[j], aux[j], w);
 #else
             amean[j] = mean_time(amean[j], aux[j], dt, elapsed);
 #endif
@@ -666,6 +691,9 @@ struct Observer {
     realtype c[N_VAR];  // neighbourhood centre
     Extent ext;
     realtype xrange[N_VAR];
+#if CLODE_SHARED_DIV
+    realtype xrange_inv[N_VAR];  // 1 / xrange (approximate-division builds)
+#endif
     realtype tex_list[NSE1];
     Stat3 npk, period, hstat;
     realtype t_start, x_thresh;
@@ -680,6 +708,9 @@ struct Observer {
         for (int j = 0; j < N_VAR; ++j) {
             c[j] = x[j];
             xrange[j] = ZERO;
+#if CLODE_SHARED_DIV
+            xrange_inv[j] = ZERO;
+#endif
         }
 #pragma unroll
         for (int j = 0; j < NSE1; ++j)
@@ -700,8 +731,12 @@ struct Observer {
     __device__ __forceinline__ void arm(CLODE_HOOK_ARGS)
     {
 #pragma unroll
-        for (int j = 0; j < N_VAR; ++j)
+        for (int j = 0; j < N_VAR; ++j) {
             xrange[j] = ext.xmax[j] - ext.xmin[j];
+#if CLODE_SHARED_DIV
+            xrange_inv[j] = ONE / xrange[j];
+#endif
+        }
         x_thresh = sel(ext.xmin, op.eVarIx) + op.xDownThresh * sel(xrange, op.eVarIx);
     }
     __device__ __forceinline__ void update(CLODE_HOOK_ARGS)
@@ -780,7 +815,11 @@ struct Observer {
         realtype acc = ZERO;
 #pragma unroll
         for (int j = 0; j < N_VAR; ++j) {
+#if CLODE_SHARED_DIV
+            realtype d = (x[j] - c[j]) * xrange_inv[j];
+#else
             realtype d = (x[j] - c[j]) / xrange[j];
+#endif
             acc += d * d;
         }
         unsigned int was_inside = inside;

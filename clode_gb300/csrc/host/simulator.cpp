@@ -491,6 +491,7 @@ struct clode_sim {
                      std::string("-DCLODE_PAIRED=") + (paired ? "1" : "0"),
                      std::string("-DCLODE_FMAD=") + (fmad ? "1" : "0"),
                      std::string("-DCLODE_FTZ=") + (ftz || fast_math ? "1" : "0"),
+                     std::string("-DCLODE_PREC_DIV=") + (prec_div && !fast_math ? "1" : "0"),
                      std::string("-DCLODE_PRECISE=") + (precise ? "1" : "0"),
                      "-DCLODE_STEP_BLOCK=" + std::to_string(step_block)};
         if (kind == CLODE_SIM_FEATURES) {
