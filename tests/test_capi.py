@@ -144,6 +144,52 @@ def test_nvrtc_builds_for_sm103a_without_spills(stepper, observer, single):
         N.lib.clode_sim_destroy(h)
 
 
+def _build_log(h):
+    n = C.c_size_t()
+    N.lib.clode_sim_get_string(h, N.STRING_BUILD_LOG, None, 0, C.byref(n))
+    b = C.create_string_buffer(n.value + 1)
+    N.lib.clode_sim_get_string(h, N.STRING_BUILD_LOG, b, n.value + 1, C.byref(n))
+    return b.value.decode()
+
+
+@pytest.mark.parametrize("paired", [1, 0])
+@pytest.mark.parametrize("model,observer", [("lactotroph.cl", "nhood2"), ("lorenz.cl", "thresh2"),
+                                            ("lorenz.cl", "nhood2")])
+def test_fast_builds_compile_for_sm103a(model, observer, paired):
+    """The benchmarked kind of build (contraction on, approximate division,
+    denormals flushed): Dormand-Prince stage sums paired two variables per
+    instruction (four variables: two pairs; three: a pair and a single) or
+    scalar, and one division per step in the observer hooks.  ptxas runs
+    here, so the paired PTX and the shared divisions are checked without a
+    GPU; the spill rule is that of the exact builds above."""
+    if model == "lactotroph.cl":
+        cp, keep = _problem(model, 4, 3, 1, 0)
+    else:
+        cp, keep = _problem(model, 3, 3, 1, 0)
+    op = N.CObserverParams(2, 0, 100, 1, 0, 0, 0.05, 0.3, 0.2, 0, 0, 0)
+    h = C.c_void_p()
+    N.check(N.lib.clode_sim_create(N.SIM_FEATURES, C.byref(cp), b"dopri5", observer.encode(), C.byref(op), 1, 0,
+                                   C.byref(h)))
+    try:
+        for k, v in (("fmad", 1), ("prec_div", 0), ("ftz", 1), ("schedule", 1), ("paired", paired)):
+            N.check(N.lib.clode_sim_set_option(h, k.encode(), C.c_double(v)))
+        N.check(N.lib.clode_sim_build(h))
+        log = _build_log(h)
+        if log:  # empty when the program came from the on-disk cache of an earlier build without a log
+            assert "sm_103a" in log
+            per_kernel = re.findall(r"entry function '(\w+)'.*?(\d+) bytes stack frame, (\d+) bytes spill stores",
+                                    log, flags=re.S)
+            assert any(name == "clode_init_observer_record" for name, _, _ in per_kernel)
+            for name, frame, spill in per_kernel:
+                limit = 128 if name.startswith("clode_features_replay") else 0
+                assert int(spill) <= limit and int(frame) <= limit, (name, frame, spill)
+        v = C.c_double(-1)
+        N.check(N.lib.clode_sim_get_option(h, b"paired", C.byref(v)))
+        assert v.value == paired
+    finally:
+        N.lib.clode_sim_destroy(h)
+
+
 def test_broken_model_source_reports_compile_error():
     src = b"void getRHS(const realtype t, const realtype x_[], const realtype p_[], realtype dx_[], " \
           b"realtype aux_[], const realtype w_[]) { dx_[0] = undefined_symbol * x_[0]; }"
