@@ -553,13 +553,17 @@ def bench_reference_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded lactotroph parameter grid)",
-            "config": {"workload": f"lactotroph nhood2 feature map {args.grid}x{args.grid}, per-member tspan "
-                                   f"U[{args.tmin:g},{args.tmax:g}], DP45 rtol 1e-6 FP32",
-                       "grid": args.grid},
+            "config": {"workload": workload_name(args.grid, args.tmin, args.tmax), "grid": args.grid},
             "cpu_baseline": {"value": value, "unit": "points/s", "cores": threads, "kind": kind,
                              "sample": f"{args.cpu_sample} random members of the grid per step"},
             "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def workload_name(grid, tmin, tmax):
+    """The map's workload, worded the same in the lines of both arms."""
+    return (f"lactotroph nhood2 feature map {grid}x{grid} = {grid * grid} points, per-member tspan "
+            f"U[{tmin:g},{tmax:g}] ms, DP45 rtol=abstol=1e-6 FP32, observer init + features per step")
 
 
 def main():
@@ -805,9 +809,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": float(np.mean(kernel_ms)), "higher_is_better": True,
         "scaling": "strong" if args.shard else "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded lactotroph parameter grid, per-member time spans)",
-        "config": {"workload": f"lactotroph nhood2 feature map {args.grid}x{args.grid} = {n} points, per-member "
-                               f"tspan U[{args.tmin:g},{args.tmax:g}] ms, DP45 rtol=abstol=1e-6 FP32, "
-                               "observer init + features per step",
+        "config": {"workload": workload_name(args.grid, args.tmin, args.tmax),
                    "grid": args.grid, "points": n,
                    "schedule": "persistent" if sim.get_option("schedule") else "grid",
                    "block_size": args.block_size, "fmad": bool(args.fmad),
