@@ -193,19 +193,20 @@ def test_fast_builds_compile_for_sm103a(model, observer, paired):
 def test_paired_option_leaves_the_exact_build_machine_code_unchanged(tmp_path):
     """With contraction off (the build that reproduces clODE bit for bit) the
     stage sums stay scalar: the compiled program is byte for byte the same
-    with ``paired`` on and off.  With contraction on it differs (the paired
-    stage sums are in it).  Compiled programs are compared as the on-disk
+    with ``paired`` on and off, as is an FP64 build with contraction on.
+    An FP32 build with contraction on differs (the paired stage sums are in
+    it).  Compiled programs are compared as the on-disk
     cache stores them (a fresh cache directory per build)."""
     import hashlib
 
-    def cubin(options, sub):
+    def cubin(options, sub, single=1):
         d = tmp_path / sub
         d.mkdir()
         N.check(N.lib.clode_set_cache_dir(str(d).encode()))
         cp, keep = _problem("lactotroph.cl", 4, 3, 1, 0)
         op = N.CObserverParams(3, 0, 100, 1, 0, 0, 0.05, 0.3, 0.2, 0, 0, 0)
         h = C.c_void_p()
-        N.check(N.lib.clode_sim_create(N.SIM_FEATURES, C.byref(cp), b"dopri5", b"nhood2", C.byref(op), 1, 0,
+        N.check(N.lib.clode_sim_create(N.SIM_FEATURES, C.byref(cp), b"dopri5", b"nhood2", C.byref(op), single, 0,
                                        C.byref(h)))
         try:
             for k, v in options.items():
@@ -221,6 +222,8 @@ def test_paired_option_leaves_the_exact_build_machine_code_unchanged(tmp_path):
         assert cubin({"paired": 1}, "exact1") == cubin({"paired": 0}, "exact0")
         fast = {"fmad": 1, "prec_div": 0, "ftz": 1}
         assert cubin(dict(fast, paired=1), "fast1") != cubin(dict(fast, paired=0), "fast0")
+        # FP64 has no paired operations: the option changes nothing there either
+        assert cubin(dict(fmad=1, paired=1), "fp64_1", single=0) == cubin(dict(fmad=1, paired=0), "fp64_0", single=0)
     finally:
         N.check(N.lib.clode_set_cache_dir(None))
 
